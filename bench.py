@@ -1,0 +1,365 @@
+"""Benchmark: PhyloCSF region scoring on GB300 (one JSON line on rank 0).
+
+Workload (default): 58mammals tree, strategy=mle (find_init + Brent over rho),
+10,000 synthetic alignments (half coding / half noncoding ECM), lengths
+log-uniform 50-3000 codons, per-species gap+N fraction U(5%,40%), 0-20% of
+species entirely missing.  A step scores every region once (both models, full
+rho MLE).  Inputs (7.2 M columns x 58 leaves, ~0.42 GB) are larger than L2.
+
+  value       regions/s with the batch resident in HBM (device-timed, CUDA
+              events on the engine's stream)
+  e2e         the same through pcsf_score_batch with pinned host buffers
+              (upload, scoring, results back inside the timed region)
+  roofline    the pruning kernel: algorithmic FLOPs (8192(nl-2)+64(nl-1)+128
+              per column-evaluation) / its device time
+  cpu_baseline  the FP64 oracle port (the reference's loop structure, dense
+              leaves) on a bounded sample of regions, one process per core
+
+``--impl reference`` times that CPU port alone (the reference is OCaml + GSL,
+which cannot be built here).  Multi-GPU (torchrun): replicas, each rank scores
+its own workload (no data-path collective), weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "codon-column·branches/s and regions scored/s at |Δscore|≤1e-3 dB vs FP64 oracle"
+
+
+def flops_per_column(nl: int) -> int:
+    return 8192 * (nl - 2) + 64 * (nl - 1) + 128
+
+
+# ---------------------------------------------------------------- distributed
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, gpu: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu), "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU port
+def _cpu_worker(args):
+    name, lv, strategy = args
+    from oracle import oracle as O
+    from tests import helpers as H
+    O.set_sparse_leaves(False)          # the reference's dense loop
+    mc, mn, ot, tree = H.oracle_models(name)
+    t0 = time.perf_counter()
+    r = O.score_region(mc, mn, ot, strategy, H.u8_to_oracle(lv))
+    return r.score, r.status, r.evals, time.perf_counter() - t0
+
+
+def cpu_port_sample(name: str, offs, leaves, strategy: int, idx, cores: int):
+    """Score regions idx with the FP64 oracle port, one process per core (spawned)."""
+    jobs = [(name, leaves[offs[i]:offs[i + 1]].copy(), strategy) for i in idx]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        out = pool.map(_cpu_worker, jobs, chunksize=1)
+    wall = time.perf_counter() - t0
+    return out, wall
+
+
+def pick_sample(offs, n, seed=123):
+    rng = np.random.default_rng(seed)
+    R = len(offs) - 1
+    return np.sort(rng.choice(R, size=min(n, R), replace=False))
+
+
+# ---------------------------------------------------------------- reference arm
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from phylocsf_gb300 import synth
+    wl = make_workload(args, seed=0)
+    cores = args.cpu_cores or os.cpu_count() or 1
+    nb = wl.params.tree.n - 1
+    times, regions, colb = [], 0, 0
+    step = 0
+    for it in range(args.warmup + args.steps):
+        idx = pick_sample(wl.col_offsets, cores, seed=1000 + it)
+        out, wall = cpu_port_sample(wl.params.name, wl.col_offsets, wl.leaves, wl.strategy, idx, cores)
+        if it >= args.warmup:
+            times.append(wall)
+            regions += len(idx)
+            colb += int(sum(wl.col_offsets[i + 1] - wl.col_offsets[i] for i in idx)) * nb
+            step += 1
+    total = sum(times)
+    v = regions / total
+    line = {"metric": METRIC, "value": v, "unit": "regions/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * total / max(step, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": wl.name, "strategy": "mle", "tree": "58mammals", "regions": wl.n_regions},
+            "cpu_baseline": {"value": v, "unit": "regions/s", "cores": cores, "kind": "port",
+                             "sample": "%d random regions per step of the workload, one process per core, "
+                                       "FP64 oracle with the reference's dense loop" % cores},
+            "e2e": {"value": v, "unit": "regions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "column_branches_per_s": colb / total,
+            "note": "the reference is OCaml+GSL and cannot be built on this image; this arm times the C FP64 "
+                    "restatement of its loop structure"}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- our arm
+def make_workload(args, seed):
+    from phylocsf_gb300 import synth
+    if args.workload == "58mammals_mle":
+        return synth.workload_58mammals_mle(n_regions=args.regions, seed=seed)
+    if args.workload == "12flies_fixed":
+        return synth.workload_12flies_fixed(seed=seed)
+    if args.workload == "120mammals_fixed":
+        return synth.workload_120mammals_fixed(total_cols=args.cols, seed=seed)
+    if args.workload == "100vertebrates_mle":
+        return synth.workload_100vertebrates_mle(n_regions=args.regions, seed=seed)
+    raise SystemExit("unknown workload " + args.workload)
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def load_traffic(kernel: str):
+    """Per-column DRAM bytes of a kernel from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import phylocsf_gb300 as P
+
+    wl = make_workload(args, seed=rank)
+    ps = wl.params
+    nl = ps.tree.nl
+    nb = ps.tree.n - 1
+    eng = P.Engine(ps.tree, ps.S_c, ps.pi_c, ps.S_n, ps.pi_n, precision=args.precision, device=local)
+    stream = torch.cuda.ExternalStream(eng.stream_handle(), device=torch.device("cuda", local))
+    batch = eng.batch(wl.col_offsets, wl.leaves)
+
+    for _ in range(args.warmup):
+        res = eng.score(batch, wl.strategy)
+    clocks = ClockSampler(local) if rank == 0 else None
+    eng.reset_stats()
+    barrier(world)
+    torch.cuda.synchronize(local)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        res = eng.score(batch, wl.strategy)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize(local)
+    barrier(world)
+    ms = ev0.elapsed_time(ev1)
+    st = eng.stats()
+    clk = clocks.stop() if clocks else None
+    ms_max = max_over_ranks(ms, world)
+    value = world * wl.n_regions * args.steps / (ms_max / 1000.0)
+    colb_per_s = world * st["column_branches"] / (ms_max / 1000.0)
+
+    # e2e: host buffers (pinned) -> pcsf_score_batch -> results on the host
+    pin = torch.from_numpy(wl.leaves).pin_memory()
+    leaves_pinned = pin.numpy()
+    offs_pinned = torch.from_numpy(wl.col_offsets).pin_memory().numpy()
+    barrier(world)
+    torch.cuda.synchronize(local)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        res_e2e = eng.score_batch(offs_pinned, leaves_pinned, wl.strategy)
+    e1.record(stream)
+    e1.synchronize()
+    barrier(world)
+    ms_e2e = max_over_ranks(e0.elapsed_time(e1), world)
+    e2e_value = world * wl.n_regions * args.steps / (ms_e2e / 1000.0)
+    same = bool(np.array_equal(res_e2e["score"], res["score"]))
+
+    # roofline of the pruning kernel (FP32 SIMT path: CUDA-core FMA bound; reported against the
+    # measured tensor peak as the contract requires, with the FP32 FMA ceiling alongside)
+    peaks, peak_kind = load_peaks()
+    cols_evaluated = st["column_branches"] / nb
+    alg_flops = cols_evaluated * flops_per_column(nl)
+    prune_s = st["prune_ms"] / 1000.0
+    achieved_tflops = alg_flops / prune_s / 1e12 if prune_s > 0 else 0.0
+    peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
+    sm_mhz = (clk or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    launches = max(st["prune_launches"], 1)
+    traffic = load_traffic("prune_" + args.precision)
+    traffic_per_launch = (traffic * cols_evaluated / launches) if traffic else None
+
+    line = {"metric": METRIC, "value": value, "unit": "regions/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": {"fp32": "f32", "fp64": "f64"}.get(args.precision, args.precision),
+            "data": "synthetic (seeded simulation along the tree; no public benchmark exists)",
+            "config": {"workload": wl.name, "tree": ps.name, "strategy": "mle" if wl.strategy else "fixed",
+                       "regions_per_gpu": wl.n_regions, "columns_per_gpu": wl.total_cols,
+                       "precision": args.precision, "l2": "inputs larger than L2 (%.0f MB)" % (wl.leaves.nbytes / 1e6),
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "column_branches_per_s": colb_per_s,
+            "e2e": {"value": e2e_value, "unit": "regions/s", "h2d_bytes_per_step": int(wl.leaves.nbytes +
+                                                                                       wl.col_offsets.nbytes),
+                    "d2h_bytes_per_step": int(res_e2e.nbytes), "same_scores_as_resident": same},
+            "gpu_launches": int(st["kernel_launches"]),
+            "rounds_per_step": st["rounds"] / args.steps,
+            "evaluations_per_step": st["evaluations"] / args.steps,
+            "roofline": {"kernel": "k_prune<%s>" % args.precision, "bound": "tensor", "achieved": achieved_tflops,
+                         "peak": peak, "unit": "TFLOP/s", "frac": achieved_tflops / peak,
+                         "peak_kind": peak_kind + " bf16 sustained",
+                         "traffic": traffic_per_launch, "alg_flops_per_launch": alg_flops / launches,
+                         "avg_launch_ms": st["prune_ms"] / launches,
+                         "fp32_fma_peak_tflops": fp32_peak, "frac_of_fp32_fma_peak": achieved_tflops / fp32_peak},
+            "kernel_ms_per_step": {"prune": st["prune_ms"] / args.steps, "pform": st["pform_ms"] / args.steps,
+                                   "other": st["other_ms"] / args.steps},
+            "clocks": clk}
+
+    if rank == 0 and not args.no_accuracy:
+        acc = {}
+        # (a) against the FP64 GPU path on a subsample
+        sub = pick_sample(wl.col_offsets, args.fp64_regions, seed=7)
+        parts = [wl.leaves[wl.col_offsets[i]:wl.col_offsets[i + 1]] for i in sub]
+        so = np.zeros(len(sub) + 1, np.int64)
+        so[1:] = np.cumsum([p.shape[0] for p in parts])
+        e64 = P.Engine(ps.tree, ps.S_c, ps.pi_c, ps.S_n, ps.pi_n, precision="fp64", device=local)
+        r64 = e64.score_batch(so, np.concatenate(parts), wl.strategy)
+        e64.close()
+        d = np.abs(r64["score"] - res["score"][sub])
+        acc["vs_fp64_gpu"] = {"regions": int(len(sub)), "max_abs_db": float(d.max()),
+                              "median_abs_db": float(np.median(d)), "frac_le_1e-3_db": float((d <= 1e-3).mean())}
+        line["accuracy"] = acc
+    if rank == 0 and not args.no_cpu_baseline:
+        cores = args.cpu_cores or os.cpu_count() or 1
+        idx = pick_sample(wl.col_offsets, cores, seed=99)
+        out, wall = cpu_port_sample(ps.name, wl.col_offsets, wl.leaves, wl.strategy, idx, cores)
+        d = np.abs(np.array([o[0] for o in out]) - res["score"][idx])
+        cols = int(sum(wl.col_offsets[i + 1] - wl.col_offsets[i] for i in idx))
+        line["cpu_baseline"] = {"value": len(idx) / wall, "unit": "regions/s", "cores": cores, "kind": "port",
+                                "sample": "%d random regions (%d codon columns) of the workload, one process per "
+                                          "core, FP64 oracle with the reference's dense loop" % (len(idx), cols),
+                                "wall_s": wall}
+        line.setdefault("accuracy", {})["vs_fp64_oracle"] = {
+            "regions": int(len(idx)), "max_abs_db": float(d.max()), "frac_le_1e-3_db": float((d <= 1e-3).mean())}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    batch.close()
+    eng.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="58mammals_mle")
+    ap.add_argument("--regions", type=int, default=10000)
+    ap.add_argument("--cols", type=int, default=2_000_000)
+    ap.add_argument("--precision", default="fp32")
+    ap.add_argument("--fp64-regions", type=int, default=256)
+    ap.add_argument("--cpu-cores", type=int, default=0)
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,182 @@
+/*
+ * phylocsf_engine.h -- C-ABI of the GB300 (sm_103a) PhyloCSF likelihood engine.
+ *
+ * The engine replaces everything below PhyloCSF's per-region `evaluator`
+ * closure (src/PhyloCSF.ml:437-467, called at :317-322): P(t) formation from an
+ * FP64 eigendecomposition of each codon rate matrix, Felsenstein pruning, the
+ * rho maximum-likelihood search and the coding-vs-noncoding LLR in decibans.
+ * Paths cited below are relative to the mlin/PhyloCSF source tree.
+ *
+ * Conventions
+ *   - Plain C types only; the caller owns every buffer it passes in.  The
+ *     engine owns its device memory and CUDA stream.
+ *   - One engine per host thread.  Calls on one engine are serialised by the
+ *     caller; distinct engines may be used from distinct threads.
+ *   - Every call returns a status (PCSF_OK = 0).  Per-region failures are
+ *     reported in pcsf_result.status and do not fail the whole call, mirroring
+ *     the reference's per-region `exception` lines (PhyloCSF.ml:323-349).
+ *   - No CPU fallback: creating an engine without a usable GB300 fails with
+ *     PCSF_ECUDA.
+ *   - Create no engine before fork(): a CUDA context must not cross fork().
+ */
+#ifndef PHYLOCSF_ENGINE_H
+#define PHYLOCSF_ENGINE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PCSF_ABI_VERSION 1
+
+/* status codes */
+#define PCSF_OK 0
+#define PCSF_EINVAL 1     /* invalid argument (tree shape, sizes, leaf codes)       */
+#define PCSF_ECUDA 2      /* CUDA error or no usable device                          */
+#define PCSF_ENOMEM 3     /* device or host allocation failed                        */
+#define PCSF_ENEGP 4      /* expm(tQ) entry below -tol             (Q.ml:234-236)   */
+#define PCSF_EROWSUM 5    /* |sum of a P(t) row - 1| > tol         (Q.ml:243-244)   */
+#define PCSF_EDIAG 6      /* renormalised P(t) diagonal not in (0,1] (Q.ml:245)     */
+#define PCSF_EBRACKET 7   /* Brent set-up found no bracketed maximum (Fit.ml:13)   */
+#define PCSF_EEIG 8       /* eigensolver did not converge                            */
+#define PCSF_ESCALE 9     /* Q scale evaluated to <= 0             (PhyloModel.ml:98) */
+#define PCSF_ERANGE 10    /* batch larger than a fixed capacity                      */
+
+/* strategies (PhyloCSFModel.ml:138-146) */
+#define PCSF_FIXED 0      /* rho = 1                                                 */
+#define PCSF_MLE 1        /* rho maximised in [0.01, 10] by find_init + Brent        */
+
+/* arithmetic of the pruning contractions (engine flags, low byte) */
+#define PCSF_PREC_FP64 0  /* FP64 everywhere: the oracle-matched plain GPU path      */
+#define PCSF_PREC_FP32 1  /* FP32 contractions on P(t)-I, FP64 eigensystem and sums  */
+#define PCSF_PREC_TF32X3 2 /* tcgen05 TF32 hi/lo split (3 products), FP32 accumulate */
+#define PCSF_PREC_BF16X3 3 /* tcgen05 BF16 hi/lo split (3 products), FP32 accumulate */
+#define PCSF_PREC_TF32 4  /* tcgen05 single TF32 product (precision study only)      */
+
+/* engine flags, bits 8..15: CUDA device ordinal + 1 (0 = the calling thread's
+ * current device).  Every call on an engine runs on the engine's device. */
+#define PCSF_DEVICE(d) ((((int32_t)(d)) + 1) << 8)
+
+/* leaf code for a marginalised leaf (gap, N, absent species; PhyloCSF.ml:231-238) */
+#define PCSF_MARGINALIZE 64
+
+typedef struct pcsf_engine pcsf_engine;
+typedef struct pcsf_batch pcsf_batch;
+
+/* Tree in CamlPaml T order (lib/CamlPaml/T.ml:57-112): leaves 0..nl-1 in Newick
+ * left-to-right order, internal nodes numbered post-order, root = 2nl-2.
+ * parent[root] = -1; branch[i] = length of the branch leading into node i. */
+typedef struct {
+    int32_t n_leaves;
+    const int32_t *parent;  /* [2*n_leaves-1] */
+    const double *branch;   /* [2*n_leaves-2] */
+} pcsf_tree;
+
+/* One region's score (PhyloCSFModel.score, PhyloCSFModel.ml:113-146). */
+typedef struct {
+    double score;           /* decibans, 10*(lpr_c - lpr_n)/ln 10        */
+    double anc_comp_score;  /* decibans, 10*(elpr_c - elpr_n)/ln 10      */
+    double rho_c, rho_n;    /* tree scale used for each model            */
+    double lpr_c, lpr_n;    /* natural-log likelihoods                    */
+    double elpr_c, elpr_n;  /* expected log prior of the root state       */
+    int32_t status;         /* PCSF_OK or the first error for this region */
+    int32_t evals;          /* distinct likelihood evaluations, both models */
+} pcsf_result;
+
+/* Engine statistics since creation (or the last pcsf_engine_reset_stats). */
+typedef struct {
+    int64_t kernel_launches;     /* launches of this library's kernels          */
+    int64_t evaluations;         /* (region, model, rho) likelihood evaluations */
+    int64_t column_branches;     /* codon-column x branch units processed       */
+    int64_t rounds;              /* lockstep optimisation rounds                */
+    double prune_ms;             /* device time of pruning kernels              */
+    double pform_ms;             /* device time of P(t) formation kernels       */
+    double other_ms;             /* device time of the other kernels            */
+    int64_t prune_launches;
+    int64_t pform_launches;
+} pcsf_stats;
+
+/* ---------------------------------------------------------------- engine */
+
+/* Create an engine for one tree and the coding / noncoding ECMs.
+ * S_*: 64x64 row-major exchangeabilities (symmetric, zero diagonal), pi_*: 64
+ * equilibrium frequencies, as read by ECM.import_parameters (src/ECM.ml:18-72).
+ * Q is assembled and scaled as PhyloCSFModel.make_q_p14n / qscale
+ * (PhyloCSFModel.ml:11-30), eigendecomposed in FP64 on the GPU (replaces
+ * Q.Diag.of_Q, Q.ml:124-141).  The root prior is pi (PhyloCSFModel.ml:56).
+ * flags: PCSF_PREC_* in the low byte.
+ * Replaces PhyloCSFModel.make (PhyloCSFModel.ml:107-110). */
+int pcsf_engine_create(const pcsf_tree *tree, const double *S_c, const double *pi_c, const double *S_n,
+                       const double *pi_n, int32_t flags, pcsf_engine **out);
+
+/* Create an engine from explicit reversible rate matrices (no scaling applied).
+ * Q_*: 64x64 row-major rate matrices reversible with respect to eq_*; prior_*
+ * is the root distribution.  Used for models that are not ECMs (for example a
+ * smaller alphabet embedded in the 64 codon states).
+ * Replaces PhyloModel.make with explicit Q.Diag.t values (PhyloModel.ml:12-25). */
+int pcsf_engine_create_q(const pcsf_tree *tree, const double *Q_c, const double *eq_c, const double *prior_c,
+                         const double *Q_n, const double *eq_n, const double *prior_n, int32_t flags,
+                         pcsf_engine **out);
+
+void pcsf_engine_destroy(pcsf_engine *e);
+
+/* Last error message of this engine (static storage if e == NULL). */
+const char *pcsf_last_error(const pcsf_engine *e);
+
+int pcsf_engine_get_stats(const pcsf_engine *e, pcsf_stats *out);
+int pcsf_engine_reset_stats(pcsf_engine *e);
+
+/* The CUDA stream (a cudaStream_t) on which the engine launches all of its
+ * work, so that callers can time it with events on that stream.  No reference
+ * counterpart (the reference has no device). */
+int pcsf_engine_stream(const pcsf_engine *e, void **stream);
+
+/* Device eigensystem of model m (0 coding, 1 noncoding): U (64x64 row-major,
+ * eigenvectors in columns of D^1/2 Q D^-1/2) and lambda (64). */
+int pcsf_engine_eigensystem(const pcsf_engine *e, int32_t model, double *U, double *lambda);
+
+/* Form P(t) for model m at the given branch lengths (n_t of them) with the
+ * clamp / renormalise rule of Q.Diag.real_to_Pt (Q.ml:211-249).
+ * P: [n_t][64][64] row-major FP64.  Per-matrix status in status[n_t]. */
+int pcsf_engine_pt(pcsf_engine *e, int32_t model, int32_t n_t, const double *t, double *P, int32_t *status);
+
+/* ---------------------------------------------------------------- batches */
+
+/* Upload a batch of regions.  Region r is columns [col_offsets[r],
+ * col_offsets[r+1]); leaves is [total_cols][n_leaves] uint8 codon indices
+ * 16*n1+4*n2+n3 (Code.ml:140-141), PCSF_MARGINALIZE for a marginalised leaf
+ * (this packs PhyloCSF.pleaves' output, PhyloCSF.ml:219-246). */
+int pcsf_batch_create(pcsf_engine *e, int32_t n_regions, const int64_t *col_offsets, const uint8_t *leaves,
+                      pcsf_batch **out);
+void pcsf_batch_destroy(pcsf_batch *b);
+
+/* Score every region of a resident batch (PhyloCSFModel.score,
+ * PhyloCSFModel.ml:142-146, for all regions at once; MLE fits advance in
+ * lockstep rounds on the device).  out: [n_regions]. */
+int pcsf_score(pcsf_engine *e, pcsf_batch *b, int32_t strategy, pcsf_result *out);
+
+/* One-shot scoring from host buffers: upload, score, free.  This is the call
+ * a batching ForkMaybe.map would make over its region list (PhyloCSF.ml:317). */
+int pcsf_score_batch(pcsf_engine *e, int32_t n_regions, const int64_t *col_offsets, const uint8_t *leaves,
+                     int32_t strategy, pcsf_result *out);
+
+/* Log-likelihood of every region under model m at tree scale rho[r]
+ * (PhyloCSFModel.lpr_leaves, PhyloCSFModel.ml:67-82).  lpr, elpr, status:
+ * [n_regions]; elpr and status may be NULL. */
+int pcsf_lpr(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, double *lpr, double *elpr,
+             int32_t *status);
+
+/* Gradient of lpr by the adjoint (outside) pass: d lpr / d branch_i at
+ * t_i = rho*b_i for every branch (d_branch: [n_regions][2*n_leaves-2], may be
+ * NULL) and d lpr / d rho (d_rho: [n_regions]).  The reference's
+ * equivalent is PhyloEM.d_ell_dtree via branch posteriors (PhyloEM.ml:140-182,
+ * PhyloLik.ml:96-174, Q.ml:260-275); it is the backward of pcsf_lpr in the
+ * sense of an autograd.Function. */
+int pcsf_grad(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, double *lpr, double *d_branch,
+              double *d_rho, int32_t *status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PHYLOCSF_ENGINE_H */

@@ -1,0 +1,1083 @@
+// Host runtime of the likelihood engine and its C-ABI (include/phylocsf_engine.h).
+//
+// Reference behaviour restated here (paths relative to mlin/PhyloCSF):
+//   Q assembly / scaling   src/PhyloCSFModel.ml:11-30, lib/CamlPaml/PhyloModel.ml:76-84,94-106
+//   lpr_leaves             src/PhyloCSFModel.ml:67-82
+//   maximize_lpr           src/PhyloCSFModel.ml:84-99
+//   find_init              lib/CamlPaml/Fit.ml:27-48
+//   Brent maximiser        lib/CamlPaml/Fit.ml:3-24 (GSL "brent" fminimizer semantics)
+//   FixedLik / MaxLik      src/PhyloCSFModel.ml:113-146
+//
+// Every region's two fits (coding, noncoding) are independent state machines
+// that advance in lockstep rounds: each round gathers the tree scales every
+// unfinished fit needs, evaluates all of them in one batched device pass
+// (P(t) formation for each distinct (model, rho), then pruning over column
+// tiles), and feeds the results back.  Evaluations are memoised per fit by
+// exact rho, so repeated evaluations at the same point (which the reference
+// performs and which give bit-identical results) are not recomputed.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "pcsf_internal.h"
+
+using namespace pcsf;
+
+namespace {
+
+thread_local std::string g_static_error;
+
+template <typename T> struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t reserve(size_t count)
+    {
+        if (count <= n) return cudaSuccess;
+        release();
+        size_t want = std::max<size_t>(count, 1);
+        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        if (e == cudaSuccess) n = want;
+        return e;
+    }
+};
+
+template <typename T> struct HostBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    ~HostBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t reserve(size_t count)
+    {
+        if (count <= n) return cudaSuccess;
+        release();
+        size_t want = std::max<size_t>(count, 1);
+        cudaError_t e = cudaMallocHost(&p, want * sizeof(T));
+        if (e == cudaSuccess) n = want;
+        return e;
+    }
+};
+
+// SplitMix64: the stand-in for OCaml's Random in find_init (seed 0 per fit).
+inline uint64_t splitmix64(uint64_t &s)
+{
+    uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+inline double uniform01(uint64_t &s) { return (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+constexpr double GOLDEN = 0.3819660;
+constexpr double SQRT_DBL_EPS = 1.4901161193847656e-08;
+
+}  // namespace
+
+void pcsf_internal_set_error(const std::string &msg) { g_static_error = msg; }
+
+struct pcsf_engine {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[8] = {};
+    int prec = PCSF_PREC_FP32;
+    std::string err;
+
+    // tree
+    int nl = 0, n = 0, nbr = 0;
+    std::vector<int> parent, lch, rch;
+    std::vector<double> branch;
+    std::vector<SchedNode> sched;
+    int nslots = 0;
+
+    // models (host copies)
+    double U[2][K2], lam[2][K], sq[2][K], isq[2][K], wrow[2][K], prior[2][K], wlog[2][K];
+    float Uf[2][K2];
+    double tol = 1e-6;
+
+    // device copies
+    DevBuf<double> dU, dlam, dsq, disq, dwrow, dprior, dwlog, dbranch;
+    DevBuf<float> dUf;
+    DevBuf<SchedNode> dsched;
+    DevModels dm{};
+
+    // per-launch work buffers
+    DevBuf<unsigned char> Pbuf;
+    size_t pbuf_psets = 0;
+    DevBuf<PSet> dps;
+    DevBuf<Request> dreq;
+    DevBuf<WorkItem> dwi;
+    DevBuf<int32_t> dwib, dstatus;
+    DevBuf<double> dpart, dlpr, delpr;
+    HostBuf<PSet> hps;
+    HostBuf<Request> hreq;
+    HostBuf<WorkItem> hwi;
+    HostBuf<int32_t> hwib, hstatus;
+    HostBuf<double> hlpr, helpr;
+    int prune_grid = 0;
+
+    pcsf_stats stats{};
+
+    int fail(int code, const char *fmt, ...)
+    {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        err = buf;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char *what)
+    {
+        return fail(e == cudaErrorMemoryAllocation ? PCSF_ENOMEM : PCSF_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+    }
+    ~pcsf_engine()
+    {
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+struct pcsf_batch {
+    pcsf_engine *e = nullptr;
+    int nreg = 0;
+    std::vector<int64_t> offs;
+    int64_t total_cols = 0;
+    DevBuf<uint8_t> dleaves;
+};
+
+#define CK(call, what)                                      \
+    do {                                                    \
+        cudaError_t _e = (call);                            \
+        if (_e != cudaSuccess) return e->cuda_fail(_e, what); \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// Tree: validation and the register-minimal evaluation schedule.
+
+static int build_tree(pcsf_engine *e, const pcsf_tree *t)
+{
+    if (!t || !t->parent || !t->branch) return e->fail(PCSF_EINVAL, "tree: null pointer");
+    int nl = t->n_leaves;
+    if (nl < 2 || nl > MAX_LEAVES) return e->fail(PCSF_EINVAL, "tree: n_leaves=%d out of range [2,%d]", nl, MAX_LEAVES);
+    int n = 2 * nl - 1;
+    e->nl = nl;
+    e->n = n;
+    e->nbr = n - 1;
+    e->parent.assign(t->parent, t->parent + n);
+    e->branch.assign(t->branch, t->branch + n - 1);
+    e->lch.assign(n, -1);
+    e->rch.assign(n, -1);
+    if (e->parent[n - 1] != -1) return e->fail(PCSF_EINVAL, "tree: parent[root] must be -1");
+    for (int i = 0; i < n - 1; i++) {
+        int p = e->parent[i];
+        if (p < nl || p >= n || p <= i)
+            return e->fail(PCSF_EINVAL, "tree: node %d has parent %d (T order needs nl <= parent, child < parent)", i, p);
+        if (e->lch[p] < 0) e->lch[p] = i;
+        else if (e->rch[p] < 0) e->rch[p] = i;
+        else return e->fail(PCSF_EINVAL, "tree: node %d has more than two children", p);
+        double b = e->branch[i];
+        if (!(b >= 0.0) || !std::isfinite(b)) return e->fail(PCSF_EINVAL, "tree: branch %d has length %g", i, b);
+    }
+    for (int i = nl; i < n; i++)
+        if (e->rch[i] < 0) return e->fail(PCSF_EINVAL, "tree: internal node %d is not bifurcating", i);
+
+    // Sethi-Ullman need: leaf 0; internal max(na, nb+1) with na >= nb.
+    std::vector<int> need(n, 0);
+    for (int i = nl; i < n; i++) {
+        int a = need[e->lch[i]], b = need[e->rch[i]];
+        if (a < b) std::swap(a, b);
+        need[i] = std::max(std::max(a, b + 1), 1);
+    }
+    e->nslots = need[n - 1];
+    // emit post-order with the needier child first; slots from a free stack
+    e->sched.clear();
+    std::vector<int> slot_of(n, -1), free_slots;
+    for (int s = e->nslots - 1; s >= 0; s--) free_slots.push_back(s);
+    std::vector<std::pair<int, int>> stack;   // (node, state)
+    stack.push_back({n - 1, 0});
+    while (!stack.empty()) {
+        auto [i, st] = stack.back();
+        stack.pop_back();
+        if (i < nl) continue;
+        int first = e->lch[i], second = e->rch[i];
+        if (need[second] > need[first]) std::swap(first, second);
+        if (st == 0) {
+            stack.push_back({i, 1});
+            stack.push_back({second, 0});
+            stack.push_back({first, 0});
+            continue;
+        }
+        SchedNode sn{};
+        sn.node = (int16_t)i;
+        sn.lc = (int16_t)e->lch[i];
+        sn.rc = (int16_t)e->rch[i];
+        sn.lslot = (int8_t)slot_of[e->lch[i]];
+        sn.rslot = (int8_t)slot_of[e->rch[i]];
+        int out;
+        if (slot_of[first] >= 0) out = slot_of[first];
+        else if (slot_of[second] >= 0) out = slot_of[second];
+        else {
+            if (free_slots.empty()) return e->fail(PCSF_EINVAL, "tree: schedule ran out of slots");
+            out = free_slots.back();
+            free_slots.pop_back();
+        }
+        if (slot_of[first] >= 0 && slot_of[first] != out) free_slots.push_back(slot_of[first]);
+        if (slot_of[second] >= 0 && slot_of[second] != out) free_slots.push_back(slot_of[second]);
+        sn.oslot = (int8_t)out;
+        slot_of[i] = out;
+        e->sched.push_back(sn);
+    }
+    if ((int)e->sched.size() != nl - 1 || e->sched.back().node != n - 1)
+        return e->fail(PCSF_EINVAL, "tree: schedule construction failed");
+    return PCSF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Models
+
+// q_ij = s_ij pi_j, q_ii = -sum_{j != i} q_ij (ascending j), scale = -sum_i pi_i q_ii
+// (ascending i), Q /= scale -- the evaluation order of the reference's
+// expression trees (PhyloCSFModel.ml:11-30, PhyloModel.ml:76-84,94-106).
+static int assemble_q(const double *S, const double *pi, double *Q)
+{
+    for (int i = 0; i < K; i++) {
+        double tot = 0.0;
+        for (int j = 0; j < K; j++) {
+            double q = (i == j) ? 0.0 : S[i * K + j] * pi[j];
+            Q[i * K + j] = q;
+            if (i != j) tot = q + tot;
+        }
+        Q[i * K + i] = 0.0 - tot;
+    }
+    double scale = 0.0;
+    for (int i = 0; i < K; i++)
+        if (Q[i * K + i] != 0.0) scale = scale - pi[i] * Q[i * K + i];
+    if (!(scale > 0.0)) return PCSF_ESCALE;
+    for (int i = 0; i < K2; i++) Q[i] = Q[i] / scale;
+    return PCSF_OK;
+}
+
+static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2], const double *prior[2])
+{
+    // symmetric similarity transforms A = D^1/2 Q D^-1/2, eigendecomposed in FP64 on the device
+    std::vector<double> A(2 * K2);
+    for (int m = 0; m < 2; m++) {
+        for (int i = 0; i < K; i++) {
+            if (!(eq[m][i] > 0.0) || !std::isfinite(eq[m][i]))
+                return e->fail(PCSF_EINVAL, "model %d: equilibrium frequency %d is %g (must be > 0)", m, i, eq[m][i]);
+            if (!(prior[m][i] > 0.0)) return e->fail(PCSF_EINVAL, "model %d: prior %d is %g (must be > 0)", m, i, prior[m][i]);
+            e->sq[m][i] = std::sqrt(eq[m][i]);
+            e->isq[m][i] = 1.0 / e->sq[m][i];
+            e->prior[m][i] = prior[m][i];
+            e->wlog[m][i] = prior[m][i] * std::log(prior[m][i]);
+        }
+        for (int i = 0; i < K; i++)
+            for (int j = 0; j < K; j++) {
+                double aij = e->sq[m][i] * Q[m][i * K + j] / e->sq[m][j];
+                double aji = e->sq[m][j] * Q[m][j * K + i] / e->sq[m][i];
+                if (std::fabs(aij - aji) > 1e-8 * (std::fabs(aij) + std::fabs(aji)) + 1e-300)
+                    return e->fail(PCSF_EINVAL, "model %d: Q is not reversible with respect to the given equilibrium (%d,%d)", m, i, j);
+                A[m * K2 + i * K + j] = 0.5 * (aij + aji);
+            }
+    }
+    DevBuf<double> dA, dUtmp, dl;
+    DevBuf<int> dst;
+    CK(dA.reserve(2 * K2), "cudaMalloc");
+    CK(dUtmp.reserve(2 * K2), "cudaMalloc");
+    CK(dl.reserve(2 * K), "cudaMalloc");
+    CK(dst.reserve(2), "cudaMalloc");
+    CK(cudaMemcpyAsync(dA.p, A.data(), sizeof(double) * 2 * K2, cudaMemcpyHostToDevice, e->stream), "H2D Q");
+    CK(launch_jacobi(dA.p, dUtmp.p, dl.p, dst.p, 2, e->stream), "eigensolver launch");
+    e->stats.kernel_launches += 1;
+    int hst[2];
+    CK(cudaMemcpyAsync(e->U, dUtmp.p, sizeof(double) * 2 * K2, cudaMemcpyDeviceToHost, e->stream), "D2H U");
+    CK(cudaMemcpyAsync(e->lam, dl.p, sizeof(double) * 2 * K, cudaMemcpyDeviceToHost, e->stream), "D2H lambda");
+    CK(cudaMemcpyAsync(hst, dst.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, e->stream), "D2H status");
+    CK(cudaStreamSynchronize(e->stream), "eigensolver");
+    if (hst[0] || hst[1]) return e->fail(PCSF_EEIG, "eigensolver did not converge");
+
+    for (int m = 0; m < 2; m++) {
+        // w_m = sum_j U_jm sqrt(pi_j): nonzero (to rounding) only for the stationary mode
+        double nrm = 0.0;
+        for (int j = 0; j < K; j++) nrm += eq[m][j];
+        nrm = std::sqrt(nrm);
+        for (int mm = 0; mm < K; mm++) {
+            double w = 0.0;
+            for (int j = 0; j < K; j++) w += e->U[m][j * K + mm] * e->sq[m][j];
+            e->wrow[m][mm] = (std::fabs(w) > 1e-9 * nrm) ? w : 0.0;
+        }
+        for (int i = 0; i < K2; i++) e->Uf[m][i] = (float)e->U[m][i];
+    }
+    CK(e->dU.reserve(2 * K2), "cudaMalloc");
+    CK(e->dUf.reserve(2 * K2), "cudaMalloc");
+    CK(e->dlam.reserve(2 * K), "cudaMalloc");
+    CK(e->dsq.reserve(2 * K), "cudaMalloc");
+    CK(e->disq.reserve(2 * K), "cudaMalloc");
+    CK(e->dwrow.reserve(2 * K), "cudaMalloc");
+    CK(e->dprior.reserve(2 * K), "cudaMalloc");
+    CK(e->dwlog.reserve(2 * K), "cudaMalloc");
+    CK(cudaMemcpyAsync(e->dU.p, e->U, sizeof(double) * 2 * K2, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(e->dUf.p, e->Uf, sizeof(float) * 2 * K2, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(e->dlam.p, e->lam, sizeof(double) * 2 * K, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(e->dsq.p, e->sq, sizeof(double) * 2 * K, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(e->disq.p, e->isq, sizeof(double) * 2 * K, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(e->dwrow.p, e->wrow, sizeof(double) * 2 * K, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(e->dprior.p, e->prior, sizeof(double) * 2 * K, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(e->dwlog.p, e->wlog, sizeof(double) * 2 * K, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaStreamSynchronize(e->stream), "model upload");
+    e->dm.U = e->dU.p;
+    e->dm.Uf = e->dUf.p;
+    e->dm.lam = e->dlam.p;
+    e->dm.sq = e->dsq.p;
+    e->dm.isq = e->disq.p;
+    e->dm.wrow = e->dwrow.p;
+    e->dm.prior = e->dprior.p;
+    e->dm.wlog = e->dwlog.p;
+    e->dm.tol = e->tol;
+    return PCSF_OK;
+}
+
+static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t flags)
+{
+    int prec = flags & 0xff;
+    if (prec != PCSF_PREC_FP64 && prec != PCSF_PREC_FP32)
+        return e->fail(PCSF_EINVAL, "precision mode %d is not available in this build", prec);
+    e->prec = prec;
+    int ndev = 0;
+    cudaError_t ce = cudaGetDeviceCount(&ndev);
+    if (ce != cudaSuccess || ndev == 0)
+        return e->fail(PCSF_ECUDA, "no CUDA device: %s", ce != cudaSuccess ? cudaGetErrorString(ce) : "count is 0");
+    int want = ((flags >> 8) & 0xff) - 1;
+    if (want >= ndev) return e->fail(PCSF_EINVAL, "device %d requested, %d present", want, ndev);
+    if (want >= 0) CK(cudaSetDevice(want), "cudaSetDevice");
+    CK(cudaGetDevice(&e->device), "cudaGetDevice");
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, e->device), "cudaGetDeviceProperties");
+    if (!(prop.major == 10 && prop.minor == 3))
+        return e->fail(PCSF_ECUDA, "device %d (%s) is sm_%d%d; this library is built for sm_103a only", e->device,
+                       prop.name, prop.major, prop.minor);
+    CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (auto &v : e->ev) CK(cudaEventCreate(&v), "cudaEventCreate");
+    int rc = build_tree(e, tree);
+    if (rc) return rc;
+    CK(e->dbranch.reserve(e->nbr), "cudaMalloc");
+    CK(e->dsched.reserve(e->sched.size()), "cudaMalloc");
+    CK(cudaMemcpyAsync(e->dbranch.p, e->branch.data(), sizeof(double) * e->nbr, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(e->dsched.p, e->sched.data(), sizeof(SchedNode) * e->sched.size(), cudaMemcpyHostToDevice,
+                       e->stream), "H2D");
+    size_t smem = prune_smem_bytes(e->prec, e->nslots, e->nl, (int)e->sched.size());
+    if (smem > (size_t)prop.sharedMemPerBlockOptin)
+        return e->fail(PCSF_EINVAL, "tree needs %d partial slots (%zu B shared memory > %zu)", e->nslots, smem,
+                       (size_t)prop.sharedMemPerBlockOptin);
+    int per_sm = std::max(1, (int)(prop.sharedMemPerMultiprocessor / (smem + 1024)));
+    per_sm = std::min(per_sm, 8);
+    e->prune_grid = prop.multiProcessorCount * per_sm;
+    // P(t) buffer: up to 4 GiB, at most a quarter of free memory
+    size_t freeb = 0, totalb = 0;
+    CK(cudaMemGetInfo(&freeb, &totalb), "cudaMemGetInfo");
+    size_t pset_bytes = (size_t)e->nbr * K2 * (e->prec == PCSF_PREC_FP64 ? 8 : 4);
+    size_t budget = std::min<size_t>(size_t(4) << 30, freeb / 4);
+    e->pbuf_psets = std::max<size_t>(1, budget / pset_bytes);
+    return PCSF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched evaluation of (region, model, rho) requests.
+
+struct Eval {
+    double lpr, elpr;
+    int status;
+};
+
+static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &reqs_in, std::vector<Eval> &out)
+{
+    const int nreq = (int)reqs_in.size();
+    out.assign(nreq, Eval{0.0, 0.0, PCSF_OK});
+    if (nreq == 0) return PCSF_OK;
+    const int TC = prune_tile_cols(e->prec);
+
+    // work items, P-set dedup and chunking (at most pbuf_psets distinct P sets per chunk)
+    std::vector<Request> reqs(reqs_in);
+    std::vector<int> wib(nreq + 1, 0);
+    std::vector<WorkItem> wis;
+    std::vector<PSet> psets;
+    std::vector<int> chunk_req_begin, chunk_ps_begin;   // chunk boundaries
+    std::map<std::pair<int, uint64_t>, int> cur;
+    chunk_req_begin.push_back(0);
+    chunk_ps_begin.push_back(0);
+    std::vector<int> req_pset_global(nreq);
+    for (int r = 0; r < nreq; r++) {
+        Request &q = reqs[r];
+        uint64_t bits;
+        std::memcpy(&bits, &q.rho, 8);
+        auto key = std::make_pair(q.model, bits);
+        auto it = cur.find(key);
+        if (it == cur.end()) {
+            if (cur.size() == e->pbuf_psets) {
+                chunk_req_begin.push_back(r);
+                chunk_ps_begin.push_back((int)psets.size());
+                cur.clear();
+            }
+            int local = (int)cur.size();
+            cur[key] = local;
+            psets.push_back(PSet{q.model, 0, q.rho});
+            q.pset = local;
+        } else {
+            q.pset = it->second;
+        }
+        req_pset_global[r] = chunk_ps_begin.back() + q.pset;
+        int64_t c0 = b->offs[q.region], c1 = b->offs[q.region + 1];
+        wib[r] = (int)wis.size();
+        for (int64_t c = c0; c < c1; c += TC) {
+            WorkItem w;
+            w.request = r;
+            w.ncols = (int)std::min<int64_t>(TC, c1 - c);
+            w.col0 = c;
+            wis.push_back(w);
+        }
+        e->stats.column_branches += (c1 - c0) * (int64_t)e->nbr;
+    }
+    wib[nreq] = (int)wis.size();
+    chunk_req_begin.push_back(nreq);
+    chunk_ps_begin.push_back((int)psets.size());
+    const int nps = (int)psets.size(), nwi = (int)wis.size();
+    e->stats.evaluations += nreq;
+
+    CK(e->hps.reserve(nps), "cudaMallocHost");
+    CK(e->hreq.reserve(nreq), "cudaMallocHost");
+    CK(e->hwi.reserve(nwi), "cudaMallocHost");
+    CK(e->hwib.reserve(nreq + 1), "cudaMallocHost");
+    CK(e->hstatus.reserve(nps), "cudaMallocHost");
+    CK(e->hlpr.reserve(nreq), "cudaMallocHost");
+    CK(e->helpr.reserve(nreq), "cudaMallocHost");
+    CK(e->dps.reserve(nps), "cudaMalloc");
+    CK(e->dreq.reserve(nreq), "cudaMalloc");
+    CK(e->dwi.reserve(nwi), "cudaMalloc");
+    CK(e->dwib.reserve(nreq + 1), "cudaMalloc");
+    CK(e->dstatus.reserve(nps), "cudaMalloc");
+    CK(e->dpart.reserve(2 * (size_t)std::max(nwi, 1)), "cudaMalloc");
+    CK(e->dlpr.reserve(nreq), "cudaMalloc");
+    CK(e->delpr.reserve(nreq), "cudaMalloc");
+    size_t pset_bytes = (size_t)e->nbr * K2 * (e->prec == PCSF_PREC_FP64 ? 8 : 4);
+    size_t max_chunk_ps = 0;
+    for (size_t c = 0; c + 1 < chunk_ps_begin.size(); c++)
+        max_chunk_ps = std::max<size_t>(max_chunk_ps, chunk_ps_begin[c + 1] - chunk_ps_begin[c]);
+    CK(e->Pbuf.reserve(max_chunk_ps * pset_bytes), "cudaMalloc P(t) buffer");
+
+    std::memcpy(e->hps.p, psets.data(), sizeof(PSet) * nps);
+    std::memcpy(e->hreq.p, reqs.data(), sizeof(Request) * nreq);
+    if (nwi) std::memcpy(e->hwi.p, wis.data(), sizeof(WorkItem) * nwi);
+    std::memcpy(e->hwib.p, wib.data(), sizeof(int32_t) * (nreq + 1));
+    cudaStream_t s = e->stream;
+    CK(cudaMemcpyAsync(e->dps.p, e->hps.p, sizeof(PSet) * nps, cudaMemcpyHostToDevice, s), "H2D psets");
+    CK(cudaMemcpyAsync(e->dreq.p, e->hreq.p, sizeof(Request) * nreq, cudaMemcpyHostToDevice, s), "H2D requests");
+    if (nwi) CK(cudaMemcpyAsync(e->dwi.p, e->hwi.p, sizeof(WorkItem) * nwi, cudaMemcpyHostToDevice, s), "H2D work");
+    CK(cudaMemcpyAsync(e->dwib.p, e->hwib.p, sizeof(int32_t) * (nreq + 1), cudaMemcpyHostToDevice, s), "H2D wib");
+    CK(cudaMemsetAsync(e->dstatus.p, 0x7f, sizeof(int32_t) * nps, s), "memset status");
+
+    float pf_ms = 0.f, pr_ms = 0.f;
+    const int nchunks = (int)chunk_req_begin.size() - 1;
+    for (int c = 0; c < nchunks; c++) {
+        int r0 = chunk_req_begin[c], r1 = chunk_req_begin[c + 1];
+        int p0 = chunk_ps_begin[c], p1 = chunk_ps_begin[c + 1];
+        CK(cudaEventRecord(e->ev[0], s), "event");
+        CK(launch_pform(e->prec == PCSF_PREC_FP64, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, e->dm, e->Pbuf.p,
+                        e->dstatus.p + p0, s), "P(t) formation launch");
+        CK(cudaEventRecord(e->ev[1], s), "event");
+        PruneArgs pa{};
+        pa.wi = e->dwi.p + wib[r0];
+        pa.nwi = wib[r1] - wib[r0];
+        pa.req = e->dreq.p;
+        pa.leaves = b->dleaves.p;
+        pa.Pbuf = e->Pbuf.p;
+        pa.sched = e->dsched.p;
+        pa.n_internal = (int)e->sched.size();
+        pa.nl = e->nl;
+        pa.nbr = e->nbr;
+        pa.nslots = e->nslots;
+        pa.m = e->dm;
+        pa.partials = e->dpart.p + 2 * (size_t)wib[r0];
+        int grid = std::min(e->prune_grid, std::max(pa.nwi, 1));
+        CK(launch_prune(e->prec, pa, s, grid), "pruning launch");
+        CK(cudaEventRecord(e->ev[2], s), "event");
+        e->stats.pform_launches += (p1 > p0);
+        e->stats.prune_launches += (pa.nwi > 0);
+        e->stats.kernel_launches += (p1 > p0) + (pa.nwi > 0);
+        CK(cudaEventSynchronize(e->ev[2]), "pruning");
+        float t1 = 0.f, t2 = 0.f;
+        cudaEventElapsedTime(&t1, e->ev[0], e->ev[1]);
+        cudaEventElapsedTime(&t2, e->ev[1], e->ev[2]);
+        pf_ms += t1;
+        pr_ms += t2;
+    }
+    CK(cudaEventRecord(e->ev[3], s), "event");
+    CK(launch_reduce(e->dpart.p, e->dwib.p, nreq, e->dlpr.p, e->delpr.p, s), "reduce launch");
+    CK(cudaEventRecord(e->ev[4], s), "event");
+    e->stats.kernel_launches += 1;
+    CK(cudaMemcpyAsync(e->hlpr.p, e->dlpr.p, sizeof(double) * nreq, cudaMemcpyDeviceToHost, s), "D2H lpr");
+    CK(cudaMemcpyAsync(e->helpr.p, e->delpr.p, sizeof(double) * nreq, cudaMemcpyDeviceToHost, s), "D2H elpr");
+    CK(cudaMemcpyAsync(e->hstatus.p, e->dstatus.p, sizeof(int32_t) * nps, cudaMemcpyDeviceToHost, s), "D2H status");
+    CK(cudaStreamSynchronize(s), "evaluation");
+    float rd_ms = 0.f;
+    cudaEventElapsedTime(&rd_ms, e->ev[3], e->ev[4]);
+    e->stats.pform_ms += pf_ms;
+    e->stats.prune_ms += pr_ms;
+    e->stats.other_ms += rd_ms;
+    for (int r = 0; r < nreq; r++) {
+        int key = e->hstatus.p[req_pset_global[r]];
+        int st = (key >= 0 && key < 0x7f000000) ? (key & 15) : PCSF_OK;
+        out[r] = Eval{e->hlpr.p[r], e->helpr.p[r], st};
+    }
+    return PCSF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// One maximize_lpr (PhyloCSFModel.ml:84-99) as a resumable state machine.
+
+struct Fit {
+    int region = 0, model = 0;
+    int64_t ncols = 0;
+    double lo = 1e-2, hi = 10.0, init = 1.0, accuracy = 0.01;
+    int maxtries = 250;
+    enum Phase { FI_START, FI_LOOP, BR_SET, BR_V, BR_PROPOSE, BR_ACCEPT, FINAL, DONE } phase = FI_START;
+    std::deque<std::pair<double, Eval>> cache;   // deque: element addresses survive push_back
+    // find_init
+    double flo = 0, fhi = 0, x = 0, fx = 0;
+    int tries = 0;
+    uint64_t rng = 0;
+    // Brent on -lpr
+    double blo = 0, bhi = 0, bflo = 0, bfhi = 0, bx = 0, bfx = 0, w = 0, fw = 0, v = 0, fv = 0, d_keep = 0, e_keep = 0;
+    double u = 0;
+    int iters = 0;
+    // results
+    int status = PCSF_OK;
+    double rho = 0, lpr = 0, elpr = 0;
+
+    const Eval *get(double r) const
+    {
+        for (auto &c : cache)
+            if (c.first == r) return &c.second;
+        return nullptr;
+    }
+};
+
+// Advance until a value outside the cache is needed (appended to `need`) or done.
+static void advance(Fit &f, std::vector<double> &need)
+{
+    auto ask = [&](double r) -> const Eval * {
+        const Eval *ev = f.get(r);
+        if (ev) return ev;
+        if (f.ncols == 0) {   // empty region: the objective is identically 0
+            f.cache.push_back({r, Eval{0.0, 0.0, PCSF_OK}});
+            return &f.cache.back().second;
+        }
+        need.push_back(r);
+        return nullptr;
+    };
+    auto failed = [&](const Eval *ev) {
+        if (ev->status != PCSF_OK) {
+            f.status = ev->status;
+            f.phase = Fit::DONE;
+            return true;
+        }
+        return false;
+    };
+    for (;;) {
+        switch (f.phase) {
+        case Fit::FI_START: {
+            const Eval *a = ask(f.lo), *b = ask(f.hi), *c = ask(f.init);
+            if (!a || !b || !c) return;
+            if (failed(a) || failed(b) || failed(c)) return;
+            f.flo = a->lpr;
+            f.fhi = b->lpr;
+            f.x = f.init;
+            f.fx = c->lpr;
+            f.tries = 0;
+            f.rng = 0;
+            f.phase = Fit::FI_LOOP;
+            break;
+        }
+        case Fit::FI_LOOP: {
+            if (f.tries < f.maxtries && (f.fx <= f.flo || f.fx <= f.fhi)) {
+                // speculatively request the next few restart points of the deterministic stream
+                const double width = std::log(f.hi) - std::log(f.lo);
+                uint64_t s = f.rng;
+                double cand = std::exp(std::log(f.lo) + uniform01(s) * width);
+                const Eval *ev = f.get(cand);
+                if (!ev && f.ncols == 0) ev = ask(cand);
+                if (!ev) {
+                    uint64_t s2 = f.rng;
+                    int k = 0;
+                    for (int t = f.tries; t < f.maxtries && k < 16; t++, k++) {
+                        double c2 = std::exp(std::log(f.lo) + uniform01(s2) * width);
+                        if (!f.get(c2)) need.push_back(c2);
+                    }
+                    return;
+                }
+                if (failed(ev)) return;
+                f.rng = s;
+                f.x = cand;
+                f.fx = ev->lpr;
+                f.tries++;
+                break;
+            }
+            if (f.tries == f.maxtries) f.x = (f.flo > f.fhi) ? f.lo : f.hi;
+            if (f.lo < f.x && f.x < f.hi) f.phase = Fit::BR_SET;
+            else f.phase = Fit::FINAL;
+            break;
+        }
+        case Fit::BR_SET: {
+            const Eval *a = ask(f.lo), *b = ask(f.hi), *c = ask(f.x);
+            if (!a || !b || !c) return;
+            if (failed(a) || failed(b) || failed(c)) return;
+            f.blo = f.lo;
+            f.bhi = f.hi;
+            f.bflo = -a->lpr;
+            f.bfhi = -b->lpr;
+            f.bx = f.x;
+            f.bfx = -c->lpr;
+            if (!(f.bfx < f.bflo && f.bfx < f.bfhi)) {
+                f.status = PCSF_EBRACKET;
+                f.phase = Fit::DONE;
+                return;
+            }
+            f.v = f.w = f.blo + GOLDEN * (f.bhi - f.blo);
+            f.phase = Fit::BR_V;
+            break;
+        }
+        case Fit::BR_V: {
+            const Eval *a = ask(f.v);
+            if (!a) return;
+            if (failed(a)) return;
+            f.fv = f.fw = -a->lpr;
+            f.d_keep = f.e_keep = 0.0;
+            f.iters = 0;
+            f.phase = Fit::BR_PROPOSE;
+            break;
+        }
+        case Fit::BR_PROPOSE: {
+            // parabolic step through (x, w, v) if acceptable, else golden section;
+            // the two remembered step lengths swap slots between iterations as
+            // in the GSL implementation the reference drives
+            const double z = f.bx, fz = f.bfx;
+            double d = f.e_keep, ee = f.d_keep;
+            const double tol = SQRT_DBL_EPS * std::fabs(z);
+            const double mid = 0.5 * (f.blo + f.bhi);
+            const double left = z - f.blo, right = f.bhi - z;
+            double p = 0.0, q = 0.0, r = 0.0;
+            if (std::fabs(ee) > tol) {
+                r = (z - f.w) * (fz - f.fv);
+                q = (z - f.v) * (fz - f.fw);
+                p = (z - f.v) * q - (z - f.w) * r;
+                q = 2.0 * (q - r);
+                if (q > 0.0) p = -p;
+                else q = -q;
+                r = ee;
+                ee = d;
+            }
+            if (std::fabs(p) < std::fabs(0.5 * q * r) && p < q * left && p < q * right) {
+                d = p / q;
+                double uu = z + d;
+                if ((uu - f.blo) < 2.0 * tol || (f.bhi - uu) < 2.0 * tol) d = (z < mid) ? tol : -tol;
+            } else {
+                ee = (z < mid) ? (f.bhi - z) : -(z - f.blo);
+                d = GOLDEN * ee;
+            }
+            f.u = (std::fabs(d) >= tol) ? z + d : z + ((d > 0.0) ? tol : -tol);
+            f.e_keep = ee;
+            f.d_keep = d;
+            f.phase = Fit::BR_ACCEPT;
+            break;
+        }
+        case Fit::BR_ACCEPT: {
+            const Eval *a = ask(f.u);
+            if (!a) return;
+            if (failed(a)) return;
+            const double u = f.u, fu = -a->lpr;
+            if (fu <= f.bfx) {
+                if (u < f.bx) { f.bhi = f.bx; f.bfhi = f.bfx; }
+                else { f.blo = f.bx; f.bflo = f.bfx; }
+                f.v = f.w; f.fv = f.fw;
+                f.w = f.bx; f.fw = f.bfx;
+                f.bx = u; f.bfx = fu;
+            } else {
+                if (u < f.bx) { f.blo = u; f.bflo = fu; }
+                else { f.bhi = u; f.bfhi = fu; }
+                if (fu <= f.fw || f.w == f.bx) {
+                    f.v = f.w; f.fv = f.fw;
+                    f.w = u; f.fw = fu;
+                } else if (fu <= f.fv || f.v == f.bx || f.v == f.w) {
+                    f.v = u; f.fv = fu;
+                }
+            }
+            f.iters++;
+            if ((f.bhi - f.blo) / f.bx > f.accuracy && f.iters < 1000) f.phase = Fit::BR_PROPOSE;
+            else {
+                f.x = f.bx;
+                f.phase = Fit::FINAL;
+            }
+            break;
+        }
+        case Fit::FINAL: {
+            const Eval *a = ask(f.x);
+            if (!a) return;
+            if (failed(a)) return;
+            f.rho = f.x;
+            f.lpr = a->lpr;
+            f.elpr = a->elpr;
+            f.phase = Fit::DONE;
+            return;
+        }
+        case Fit::DONE:
+            return;
+        }
+    }
+}
+
+static double decibans(double x) { return 10.0 * x / std::log(10.0); }
+
+static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
+{
+    std::vector<Request> reqs;
+    std::vector<std::pair<int, double>> owner;
+    std::vector<Eval> res;
+    for (;;) {
+        reqs.clear();
+        owner.clear();
+        for (int i = 0; i < (int)fits.size(); i++) {
+            std::vector<double> need;
+            advance(fits[i], need);
+            std::sort(need.begin(), need.end());
+            need.erase(std::unique(need.begin(), need.end()), need.end());
+            for (double r : need) {
+                if (!(r > 0.0) || !std::isfinite(r)) {
+                    fits[i].status = PCSF_EINVAL;
+                    fits[i].phase = Fit::DONE;
+                    break;
+                }
+                Request q{};
+                q.region = fits[i].region;
+                q.model = fits[i].model;
+                q.rho = r;
+                reqs.push_back(q);
+                owner.push_back({i, r});
+            }
+        }
+        if (reqs.empty()) break;
+        e->stats.rounds += 1;
+        int rc = evaluate(e, b, reqs, res);
+        if (rc) return rc;
+        for (size_t k = 0; k < reqs.size(); k++) fits[owner[k].first].cache.push_back({owner[k].second, res[k]});
+    }
+    return PCSF_OK;
+}
+
+static int score_impl(pcsf_engine *e, pcsf_batch *b, int strategy, pcsf_result *out)
+{
+    if (strategy != PCSF_FIXED && strategy != PCSF_MLE) return e->fail(PCSF_EINVAL, "strategy %d", strategy);
+    const int nreg = b->nreg;
+    std::vector<Fit> fits(2 * (size_t)nreg);
+    for (int r = 0; r < nreg; r++)
+        for (int m = 0; m < 2; m++) {
+            Fit &f = fits[2 * r + m];
+            f.region = r;
+            f.model = m;
+            f.ncols = b->offs[r + 1] - b->offs[r];
+            if (strategy == PCSF_FIXED) {
+                // llr_FixedLik 1.0: a single evaluation at rho = 1
+                f.x = 1.0;
+                f.phase = Fit::FINAL;
+            }
+        }
+    int rc = run_fits(e, b, fits);
+    if (rc) return rc;
+    for (int r = 0; r < nreg; r++) {
+        const Fit &c = fits[2 * r], &nf = fits[2 * r + 1];
+        pcsf_result &o = out[r];
+        std::memset(&o, 0, sizeof o);
+        o.status = c.status != PCSF_OK ? c.status : nf.status;
+        o.rho_c = c.rho;
+        o.rho_n = nf.rho;
+        o.lpr_c = c.lpr;
+        o.lpr_n = nf.lpr;
+        o.elpr_c = c.elpr;
+        o.elpr_n = nf.elpr;
+        o.score = decibans(c.lpr - nf.lpr);
+        o.anc_comp_score = decibans(c.elpr - nf.elpr);
+        o.evals = (int32_t)(c.cache.size() + nf.cache.size());
+    }
+    return PCSF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C-ABI
+
+extern "C" {
+
+int pcsf_engine_create(const pcsf_tree *tree, const double *S_c, const double *pi_c, const double *S_n,
+                       const double *pi_n, int32_t flags, pcsf_engine **out)
+{
+    if (!out) {
+        g_static_error = "pcsf_engine_create: out is NULL";
+        return PCSF_EINVAL;
+    }
+    *out = nullptr;
+    if (!S_c || !pi_c || !S_n || !pi_n) {
+        g_static_error = "pcsf_engine_create: null model pointer";
+        return PCSF_EINVAL;
+    }
+    double Q[2][K2];
+    const double *S[2] = {S_c, S_n}, *pi[2] = {pi_c, pi_n};
+    for (int m = 0; m < 2; m++) {
+        if (assemble_q(S[m], pi[m], Q[m]) != PCSF_OK) {
+            g_static_error = "CamlPaml.P14n.instantiate_q: Q scale evaluated to a non-positive value";
+            return PCSF_ESCALE;
+        }
+    }
+    const double *Qp[2] = {Q[0], Q[1]};
+    return pcsf_engine_create_q(tree, Qp[0], pi_c, pi_c, Qp[1], pi_n, pi_n, flags, out);
+}
+
+int pcsf_engine_create_q(const pcsf_tree *tree, const double *Q_c, const double *eq_c, const double *prior_c,
+                         const double *Q_n, const double *eq_n, const double *prior_n, int32_t flags,
+                         pcsf_engine **out)
+{
+    if (!out) {
+        g_static_error = "pcsf_engine_create_q: out is NULL";
+        return PCSF_EINVAL;
+    }
+    *out = nullptr;
+    if (!Q_c || !eq_c || !prior_c || !Q_n || !eq_n || !prior_n) {
+        g_static_error = "pcsf_engine_create_q: null model pointer";
+        return PCSF_EINVAL;
+    }
+    pcsf_engine *e = new (std::nothrow) pcsf_engine();
+    if (!e) {
+        g_static_error = "out of host memory";
+        return PCSF_ENOMEM;
+    }
+    int rc = engine_init_common(e, tree, flags);
+    if (rc == PCSF_OK) {
+        const double *Q[2] = {Q_c, Q_n}, *eq[2] = {eq_c, eq_n}, *pr[2] = {prior_c, prior_n};
+        rc = setup_models(e, Q, eq, pr);
+    }
+    if (rc != PCSF_OK) {
+        g_static_error = e->err;
+        delete e;
+        return rc;
+    }
+    *out = e;
+    return PCSF_OK;
+}
+
+void pcsf_engine_destroy(pcsf_engine *e)
+{
+    if (e) cudaSetDevice(e->device);
+    delete e;
+}
+
+const char *pcsf_last_error(const pcsf_engine *e) { return e ? e->err.c_str() : g_static_error.c_str(); }
+
+int pcsf_engine_get_stats(const pcsf_engine *e, pcsf_stats *out)
+{
+    if (!e || !out) return PCSF_EINVAL;
+    *out = e->stats;
+    return PCSF_OK;
+}
+
+int pcsf_engine_reset_stats(pcsf_engine *e)
+{
+    if (!e) return PCSF_EINVAL;
+    e->stats = pcsf_stats{};
+    return PCSF_OK;
+}
+
+int pcsf_engine_stream(const pcsf_engine *e, void **stream)
+{
+    if (!e || !stream) return PCSF_EINVAL;
+    *stream = (void *)e->stream;
+    return PCSF_OK;
+}
+
+int pcsf_engine_eigensystem(const pcsf_engine *e, int32_t model, double *U, double *lambda)
+{
+    if (!e || model < 0 || model > 1 || !U || !lambda) return PCSF_EINVAL;
+    std::memcpy(U, e->U[model], sizeof(double) * K2);
+    std::memcpy(lambda, e->lam[model], sizeof(double) * K);
+    return PCSF_OK;
+}
+
+int pcsf_engine_pt(pcsf_engine *e, int32_t model, int32_t n_t, const double *t, double *P, int32_t *status)
+{
+    if (!e) return PCSF_EINVAL;
+    CK(cudaSetDevice(e->device), "cudaSetDevice");
+    if (model < 0 || model > 1 || n_t <= 0 || !t || !P || !status) return e->fail(PCSF_EINVAL, "pcsf_engine_pt: bad argument");
+    for (int i = 0; i < n_t; i++)
+        if (!(t[i] >= 0.0) || !std::isfinite(t[i])) return e->fail(PCSF_EINVAL, "pcsf_engine_pt: t[%d] = %g", i, t[i]);
+    const bool fp64 = e->prec == PCSF_PREC_FP64;
+    const size_t es = fp64 ? 8 : 4;
+    DevBuf<double> dt;
+    DevBuf<unsigned char> dP;
+    DevBuf<PSet> dps;
+    DevBuf<int32_t> dst;
+    CK(dt.reserve(n_t), "cudaMalloc");
+    CK(dP.reserve((size_t)n_t * K2 * es), "cudaMalloc");
+    CK(dps.reserve(1), "cudaMalloc");
+    CK(dst.reserve(1), "cudaMalloc");
+    PSet ps{model, 0, 1.0};
+    CK(cudaMemcpyAsync(dt.p, t, sizeof(double) * n_t, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(dps.p, &ps, sizeof ps, cudaMemcpyHostToDevice, e->stream), "H2D");
+    std::vector<int32_t> keys(n_t, STATUS_NONE);
+    // one launch per matrix so that each gets its own status key
+    std::vector<unsigned char> raw((size_t)n_t * K2 * es);
+    for (int i = 0; i < n_t; i++) {
+        CK(cudaMemsetAsync(dst.p, 0x7f, sizeof(int32_t), e->stream), "memset");
+        CK(launch_pform(fp64, dps.p, 1, dt.p + i, 1, e->dm, dP.p + (size_t)i * K2 * es, dst.p, e->stream), "P(t) launch");
+        e->stats.kernel_launches += 1;
+        CK(cudaMemcpyAsync(&keys[i], dst.p, sizeof(int32_t), cudaMemcpyDeviceToHost, e->stream), "D2H");
+    }
+    CK(cudaMemcpyAsync(raw.data(), dP.p, raw.size(), cudaMemcpyDeviceToHost, e->stream), "D2H P");
+    CK(cudaStreamSynchronize(e->stream), "P(t)");
+    for (int i = 0; i < n_t; i++) {
+        status[i] = (keys[i] >= 0 && keys[i] < 0x7f000000) ? (keys[i] & 15) : PCSF_OK;
+        for (int r = 0; r < K; r++)
+            for (int c = 0; c < K; c++) {
+                size_t src = (size_t)i * K2 + (size_t)c * K + r;   // stored as E^T
+                double ev = fp64 ? reinterpret_cast<double *>(raw.data())[src] : reinterpret_cast<float *>(raw.data())[src];
+                P[(size_t)i * K2 + r * K + c] = ev + (r == c ? 1.0 : 0.0);
+            }
+    }
+    return PCSF_OK;
+}
+
+int pcsf_batch_create(pcsf_engine *e, int32_t n_regions, const int64_t *col_offsets, const uint8_t *leaves,
+                      pcsf_batch **out)
+{
+    if (!e) return PCSF_EINVAL;
+    CK(cudaSetDevice(e->device), "cudaSetDevice");
+    if (!out) return e->fail(PCSF_EINVAL, "pcsf_batch_create: out is NULL");
+    *out = nullptr;
+    if (n_regions < 0 || (n_regions > 0 && !col_offsets)) return e->fail(PCSF_EINVAL, "pcsf_batch_create: bad regions");
+    pcsf_batch *b = new (std::nothrow) pcsf_batch();
+    if (!b) return e->fail(PCSF_ENOMEM, "out of host memory");
+    b->e = e;
+    b->nreg = n_regions;
+    b->offs.assign(n_regions + 1, 0);
+    if (n_regions > 0) {
+        if (col_offsets[0] != 0) {
+            delete b;
+            return e->fail(PCSF_EINVAL, "pcsf_batch_create: col_offsets[0] must be 0");
+        }
+        for (int r = 0; r <= n_regions; r++) {
+            b->offs[r] = col_offsets[r];
+            if (r > 0 && col_offsets[r] < col_offsets[r - 1]) {
+                delete b;
+                return e->fail(PCSF_EINVAL, "pcsf_batch_create: col_offsets not non-decreasing at %d", r);
+            }
+        }
+    }
+    b->total_cols = b->offs[n_regions];
+    if (b->total_cols > 0 && !leaves) {
+        delete b;
+        return e->fail(PCSF_EINVAL, "pcsf_batch_create: leaves is NULL");
+    }
+    const size_t nbytes = (size_t)b->total_cols * e->nl;
+    for (size_t i = 0; i < nbytes; i++)
+        if (leaves[i] > PCSF_MARGINALIZE) {
+            size_t col = i / e->nl;
+            int lf = (int)(i % e->nl);
+            delete b;
+            return e->fail(PCSF_EINVAL, "pcsf_batch_create: leaf code %d at column %zu leaf %d (max %d)", leaves[i], col,
+                           lf, PCSF_MARGINALIZE);
+        }
+    cudaError_t ce = b->dleaves.reserve(nbytes + 16);
+    if (ce == cudaSuccess && nbytes)
+        ce = cudaMemcpyAsync(b->dleaves.p, leaves, nbytes, cudaMemcpyHostToDevice, e->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) {
+        delete b;
+        return e->cuda_fail(ce, "batch upload");
+    }
+    *out = b;
+    return PCSF_OK;
+}
+
+void pcsf_batch_destroy(pcsf_batch *b)
+{
+    if (b && b->e) cudaSetDevice(b->e->device);
+    delete b;
+}
+
+int pcsf_score(pcsf_engine *e, pcsf_batch *b, int32_t strategy, pcsf_result *out)
+{
+    if (!e) return PCSF_EINVAL;
+    CK(cudaSetDevice(e->device), "cudaSetDevice");
+    if (!b || b->e != e) return e->fail(PCSF_EINVAL, "pcsf_score: batch does not belong to this engine");
+    if (b->nreg > 0 && !out) return e->fail(PCSF_EINVAL, "pcsf_score: out is NULL");
+    return score_impl(e, b, strategy, out);
+}
+
+int pcsf_score_batch(pcsf_engine *e, int32_t n_regions, const int64_t *col_offsets, const uint8_t *leaves,
+                     int32_t strategy, pcsf_result *out)
+{
+    pcsf_batch *b = nullptr;
+    int rc = pcsf_batch_create(e, n_regions, col_offsets, leaves, &b);
+    if (rc) return rc;
+    rc = pcsf_score(e, b, strategy, out);
+    pcsf_batch_destroy(b);
+    return rc;
+}
+
+int pcsf_lpr(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, double *lpr, double *elpr,
+             int32_t *status)
+{
+    if (!e) return PCSF_EINVAL;
+    CK(cudaSetDevice(e->device), "cudaSetDevice");
+    if (!b || b->e != e) return e->fail(PCSF_EINVAL, "pcsf_lpr: batch does not belong to this engine");
+    if (model < 0 || model > 1) return e->fail(PCSF_EINVAL, "pcsf_lpr: model %d", model);
+    if (b->nreg > 0 && (!rho || !lpr)) return e->fail(PCSF_EINVAL, "pcsf_lpr: null output");
+    std::vector<Request> reqs(b->nreg);
+    for (int r = 0; r < b->nreg; r++) {
+        if (!(rho[r] > 0.0) || !std::isfinite(rho[r])) return e->fail(PCSF_EINVAL, "pcsf_lpr: rho[%d] = %g", r, rho[r]);
+        reqs[r] = Request{r, model, 0, 0, rho[r]};
+    }
+    std::vector<Eval> res;
+    int rc = evaluate(e, b, reqs, res);
+    if (rc) return rc;
+    for (int r = 0; r < b->nreg; r++) {
+        lpr[r] = res[r].lpr;
+        if (elpr) elpr[r] = res[r].elpr;
+        if (status) status[r] = res[r].status;
+    }
+    return PCSF_OK;
+}
+
+int pcsf_grad(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, double *lpr, double *d_branch,
+              double *d_rho, int32_t *status)
+{
+    (void)b; (void)model; (void)rho; (void)lpr; (void)d_branch; (void)d_rho; (void)status;
+    if (!e) return PCSF_EINVAL;
+    return e->fail(PCSF_EINVAL, "pcsf_grad: the adjoint kernel is not built yet");
+}
+
+}  // extern "C"

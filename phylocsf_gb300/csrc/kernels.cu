@@ -1,0 +1,579 @@
+// SIMT kernels of the likelihood engine: FP64 eigensolver, P(t) formation,
+// Felsenstein pruning (FP64 and FP32) and the per-request reduction.
+//
+// Reference behaviour restated here (paths relative to mlin/PhyloCSF):
+//   eigendecomposition  lib/CamlPaml/Q.ml:124-141 (GSL nonsymmv + complex LU in the
+//                       reference; a parallel cyclic Jacobi on D^1/2 Q D^-1/2 here)
+//   P(t) + row rule     lib/CamlPaml/Q.ml:211-249
+//   inside pass         lib/CamlPaml/PhyloLik.ml:73-93
+//   root posterior      lib/CamlPaml/PhyloLik.ml:127-138, src/PhyloCSFModel.ml:67-82
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+
+#include "pcsf_internal.h"
+
+namespace pcsf {
+
+// ---------------------------------------------------------------------------
+// Eigensolver: one CTA per symmetric 64x64 matrix, 256 threads.  Each Jacobi
+// sweep visits all 2016 pairs as 63 rounds of 32 disjoint rotations (round-robin
+// "circle" ordering), which are applied simultaneously.
+
+constexpr int JAC_THREADS = 256;
+constexpr int JAC_LD = K + 1;
+
+__device__ inline void jac_pair(int r, int i, int &p, int &q)
+{
+    int a, b;
+    if (i == 0) { a = K - 1; b = r; }
+    else { a = (r + i) % (K - 1); b = (r - i + (K - 1)) % (K - 1); }
+    p = a < b ? a : b;
+    q = a < b ? b : a;
+}
+
+__global__ void __launch_bounds__(JAC_THREADS) k_jacobi(const double *A_in, double *U_out, double *lam_out,
+                                                         int *status)
+{
+    extern __shared__ __align__(16) unsigned char jsm[];
+    double *A = reinterpret_cast<double *>(jsm);      // [K][JAC_LD]
+    double *V = A + K * JAC_LD;                        // [K][JAC_LD]
+    double *red = V + K * JAC_LD;                      // [JAC_THREADS]
+    double *cs = red + JAC_THREADS;                    // [32]
+    double *sn = cs + 32;                              // [32]
+    int *pp = reinterpret_cast<int *>(sn + 32);        // [32]
+    int *qq = pp + 32;                                 // [32]
+    const int tid = threadIdx.x;
+    const double *Ain = A_in + (size_t)blockIdx.x * K2;
+
+    for (int f = tid; f < K2; f += JAC_THREADS) {
+        int i = f / K, j = f % K;
+        A[i * JAC_LD + j] = Ain[f];
+        V[i * JAC_LD + j] = (i == j) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    // ||A||_F^2 (fixed-order tree reduction)
+    double part = 0.0;
+    for (int f = tid; f < K2; f += JAC_THREADS) {
+        double x = A[(f / K) * JAC_LD + f % K];
+        part += x * x;
+    }
+    red[tid] = part;
+    __syncthreads();
+    for (int w = JAC_THREADS / 2; w > 0; w >>= 1) {
+        if (tid < w) red[tid] += red[tid + w];
+        __syncthreads();
+    }
+    const double norm2 = red[0];
+    __syncthreads();
+
+    int converged = 0;
+    for (int sweep = 0; sweep < 60; sweep++) {
+        part = 0.0;
+        for (int f = tid; f < K2; f += JAC_THREADS) {
+            int i = f / K, j = f % K;
+            if (i < j) { double x = A[i * JAC_LD + j]; part += x * x; }
+        }
+        red[tid] = part;
+        __syncthreads();
+        for (int w = JAC_THREADS / 2; w > 0; w >>= 1) {
+            if (tid < w) red[tid] += red[tid + w];
+            __syncthreads();
+        }
+        double off = red[0];
+        __syncthreads();
+        if (off <= 1e-32 * norm2) { converged = 1; break; }
+        for (int r = 0; r < K - 1; r++) {
+            if (tid < 32) {
+                int p, q;
+                jac_pair(r, tid, p, q);
+                double apq = A[p * JAC_LD + q];
+                double c = 1.0, s = 0.0;
+                if (apq != 0.0) {
+                    double theta = (A[q * JAC_LD + q] - A[p * JAC_LD + p]) / (2.0 * apq);
+                    double t = (fabs(theta) > 1e150) ? 0.5 / theta
+                               : (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                    c = 1.0 / sqrt(t * t + 1.0);
+                    s = t * c;
+                }
+                cs[tid] = c; sn[tid] = s; pp[tid] = p; qq[tid] = q;
+            }
+            __syncthreads();
+            for (int f = tid; f < K * 32; f += JAC_THREADS) {       // columns: A <- A J, V <- V J
+                int row = f >> 5, k = f & 31;
+                int p = pp[k], q = qq[k];
+                double c = cs[k], s = sn[k];
+                double a = A[row * JAC_LD + p], b = A[row * JAC_LD + q];
+                A[row * JAC_LD + p] = c * a - s * b;
+                A[row * JAC_LD + q] = s * a + c * b;
+                double va = V[row * JAC_LD + p], vb = V[row * JAC_LD + q];
+                V[row * JAC_LD + p] = c * va - s * vb;
+                V[row * JAC_LD + q] = s * va + c * vb;
+            }
+            __syncthreads();
+            for (int f = tid; f < K * 32; f += JAC_THREADS) {       // rows: A <- J^T A
+                int col = f >> 5, k = f & 31;
+                int p = pp[k], q = qq[k];
+                double c = cs[k], s = sn[k];
+                double a = A[p * JAC_LD + col], b = A[q * JAC_LD + col];
+                A[p * JAC_LD + col] = c * a - s * b;
+                A[q * JAC_LD + col] = s * a + c * b;
+            }
+            __syncthreads();
+            if (tid < 32) {
+                A[pp[tid] * JAC_LD + qq[tid]] = 0.0;
+                A[qq[tid] * JAC_LD + pp[tid]] = 0.0;
+            }
+            __syncthreads();
+        }
+    }
+    double *Uo = U_out + (size_t)blockIdx.x * K2;
+    for (int f = tid; f < K2; f += JAC_THREADS) Uo[f] = V[(f / K) * JAC_LD + f % K];
+    if (tid < K) lam_out[(size_t)blockIdx.x * K + tid] = A[tid * JAC_LD + tid];
+    if (tid == 0) status[blockIdx.x] = converged ? 0 : 1;
+}
+
+cudaError_t launch_jacobi(const double *A, double *U, double *lam, int *status, int nmat, cudaStream_t s)
+{
+    size_t smem = sizeof(double) * (2 * K * JAC_LD + JAC_THREADS + 64) + sizeof(int) * 64;
+    cudaError_t err = cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    k_jacobi<<<nmat, JAC_THREADS, smem, s>>>(A, U, lam, status);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// P(t) formation.  For branch b of request r at t = rho_r * b_b:
+//   E = P(t) - I = D^-1/2 U diag(expm1(lam t)) U^T D^1/2
+// (expm1 in FP64; the 64^3 product in the storage precision T), then the row
+// rule of Q.ml:226-247 on P = I + E:
+//   - the raw row sum must be within tol of 1 (evaluated in FP64 through the
+//     eigensystem identity sum_j E_ij = isq_i sum_m U_im expm1(lam_m t) w_m);
+//   - off-diagonal negatives within tol are set to 0, below -tol are an error;
+//   - the diagonal becomes 1 - sum of the off-diagonal entries, and must lie in
+//     (0,1].
+// Output is E^T: Pbuf[(r*nbr + b)*K2 + j*K + i] = E[i][j].
+
+constexpr int PF_THREADS = 256;
+constexpr int PF_BRANCHES = 4;   // branches per CTA (the eigenvectors are staged once)
+
+template <typename T> struct Vec4;
+template <> struct Vec4<float> {
+    static __device__ inline void load(const float *p, float v[4])
+    {
+        float4 x = *reinterpret_cast<const float4 *>(p);
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+    }
+};
+template <> struct Vec4<double> {
+    static __device__ inline void load(const double *p, double v[4])
+    {
+        double2 x = *reinterpret_cast<const double2 *>(p);
+        double2 y = *reinterpret_cast<const double2 *>(p + 2);
+        v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
+    }
+};
+
+__device__ inline void status_min(int32_t *key, int branch, int row, int code)
+{
+    atomicMin(key, ((branch * K + row) << 4) | code);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const double *branch, int nbr,
+                                                       DevModels m, T *Pbuf, int32_t *status_key)
+{
+    extern __shared__ __align__(16) unsigned char psm[];
+    T *UT = reinterpret_cast<T *>(psm);     // [K][K]   UT[m][j] = U[j][m]
+    T *UeT = UT + K2;                         // [K][K]   UeT[m][i] = U[i][m] * expm1(lam_m t)
+    T *Es = UeT + K2;                         // [K][K+1] E[i][j]
+    T *sqT = Es + K * (K + 1);                // [K]
+    T *isqT = sqT + K;                        // [K]
+    double *ex = reinterpret_cast<double *>(isqT + K);   // [K]
+    const int tid = threadIdx.x;
+    const int r = blockIdx.y;
+    const PSet rq = ps[r];
+    const int md = rq.model;
+    const double *U = m.U + (size_t)md * K2;
+    const float *Uf = m.Uf + (size_t)md * K2;
+    const double *lam = m.lam + md * K;
+    const double *isq = m.isq + md * K;
+    const double *wrow = m.wrow + md * K;
+
+    for (int f = tid; f < K2; f += PF_THREADS) {
+        int j = f / K, mm = f % K;   // U[j][mm]
+        UT[mm * K + j] = (sizeof(T) == 8) ? (T)U[f] : (T)Uf[f];
+    }
+    if (tid < K) {
+        sqT[tid] = (T)m.sq[md * K + tid];
+        isqT[tid] = (T)isq[tid];
+    }
+    const int ty = tid / 16, tx = tid % 16;
+    for (int bi = 0; bi < PF_BRANCHES; bi++) {
+        const int b = blockIdx.x * PF_BRANCHES + bi;
+        if (b >= nbr) break;                       // uniform across the block
+        const double t = rq.rho * branch[b];
+        __syncthreads();                           // UT ready / previous branch done with smem
+        if (tid < K) ex[tid] = expm1(lam[tid] * t);
+        __syncthreads();
+        for (int f = tid; f < K2; f += PF_THREADS) {
+            int mm = f / K;
+            UeT[f] = UT[f] * (T)ex[mm];
+        }
+        __syncthreads();
+        T acc[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) acc[i][j] = (T)0;
+        for (int mm = 0; mm < K; mm++) {
+            T a[4], bb[4];
+            Vec4<T>::load(UeT + mm * K + 4 * ty, a);
+            Vec4<T>::load(UT + mm * K + 4 * tx, bb);
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] += a[i] * bb[j];
+        }
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                int ii = 4 * ty + i, jj = 4 * tx + j;
+                Es[ii * (K + 1) + jj] = acc[i][j] * sqT[jj] * isqT[ii];
+            }
+        __syncthreads();
+        if (tid < K) {
+            const int i = tid;
+            // raw row sum - 1, in FP64 through the eigensystem
+            double rs = 0.0;
+            for (int mm = 0; mm < K; mm++) {
+                double w = wrow[mm];
+                if (w != 0.0) rs += U[i * K + mm] * ex[mm] * w;
+            }
+            rs *= isq[i];
+            bool neg = false;
+            T diag = (T)0;
+            for (int j = 0; j < K; j++) {
+                T x = Es[i * (K + 1) + j];
+                if (j == i) {
+                    if ((double)x + 1.0 < 0.0 && -((double)x + 1.0) > m.tol) neg = true;
+                    continue;
+                }
+                if (x < (T)0) {
+                    if (-(double)x > m.tol) neg = true;
+                    x = (T)0;
+                    Es[i * (K + 1) + j] = x;
+                }
+                diag -= x;
+            }
+            if (neg) status_min(status_key + r, b, i, PCSF_ENEGP);
+            else if (fabs(rs) > m.tol) status_min(status_key + r, b, i, PCSF_EROWSUM);
+            else if (!((double)diag > -1.0)) status_min(status_key + r, b, i, PCSF_EDIAG);
+            Es[i * (K + 1) + i] = diag;
+        }
+        __syncthreads();
+        T *out = Pbuf + ((size_t)r * nbr + b) * K2;
+        for (int f = tid; f < K2; f += PF_THREADS) {
+            int j = f / K, i = f % K;
+            out[f] = Es[i * (K + 1) + j];
+        }
+    }
+}
+
+cudaError_t launch_pform(bool fp64, const PSet *req, int nreq, const double *branch, int nbr, DevModels m,
+                         void *Pbuf, int32_t *status_key, cudaStream_t s)
+{
+    if (nreq <= 0) return cudaSuccess;
+    dim3 grid((nbr + PF_BRANCHES - 1) / PF_BRANCHES, nreq);
+    if (fp64) {
+        size_t smem = sizeof(double) * (2 * K2 + K * (K + 1) + 3 * K);
+        cudaError_t e = cudaFuncSetAttribute(k_pform<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_pform<double><<<grid, PF_THREADS, smem, s>>>(req, branch, nbr, m, (double *)Pbuf, status_key);
+    } else {
+        size_t smem = sizeof(float) * (2 * K2 + K * (K + 1) + 2 * K) + sizeof(double) * K;
+        smem = (smem + 15) & ~size_t(15);
+        cudaError_t e = cudaFuncSetAttribute(k_pform<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_pform<float><<<grid, PF_THREADS, smem, s>>>(req, branch, nbr, m, (float *)Pbuf, status_key);
+    }
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Pruning (inside pass).  One CTA (256 threads) owns a tile of TC columns of
+// one request's region and walks the internal nodes in the register-minimal
+// (Sethi-Ullman) schedule computed on the host; partials live in shared
+// memory slots [K][TC].  Thread (ty,tx) owns states 4ty..4ty+3 and columns
+// tx*CPT..tx*CPT+CPT-1.
+//
+// For a child c of node i:   v_c[a] = alpha_c[a] + sum_j E_c[a][j] alpha_c[j]
+// (internal child; E = P - I keeps the large diagonal exact), or the gather
+// v_c[a] = P_c[a][s] for a leaf in state s (1 for a marginalised leaf: P rows
+// sum to 1 after the row rule).  Then alpha_i = v_l * v_r, and each column is
+// rescaled by an exact power of two so its maximum lies in [0.5,1); the
+// exponents are summed per column and added back as e*ln2 in FP64 at the root.
+
+template <typename T> struct AtomMax;
+template <> struct AtomMax<float> {
+    typedef int U;
+    static __device__ inline void upd(U *p, float v) { atomicMax(p, __float_as_int(v)); }
+    static __device__ inline float get(const U *p) { return __int_as_float(*p); }
+};
+template <> struct AtomMax<double> {
+    typedef unsigned long long U;
+    static __device__ inline void upd(U *p, double v) { atomicMax(p, (unsigned long long)__double_as_longlong(v)); }
+    static __device__ inline double get(const U *p) { return __longlong_as_double((long long)*p); }
+};
+
+template <typename T, int CPT> struct ColLoad;
+template <> struct ColLoad<float, 4> {
+    static __device__ inline void load(const float *p, float v[4]) { Vec4<float>::load(p, v); }
+};
+template <> struct ColLoad<float, 2> {
+    static __device__ inline void load(const float *p, float v[2])
+    {
+        float2 x = *reinterpret_cast<const float2 *>(p);
+        v[0] = x.x; v[1] = x.y;
+    }
+};
+template <> struct ColLoad<double, 2> {
+    static __device__ inline void load(const double *p, double v[2])
+    {
+        double2 x = *reinterpret_cast<const double2 *>(p);
+        v[0] = x.x; v[1] = x.y;
+    }
+};
+template <> struct ColLoad<double, 4> {
+    static __device__ inline void load(const double *p, double v[4]) { Vec4<double>::load(p, v); }
+};
+
+__device__ inline int exp_of(float x) { int e; frexpf(x, &e); return e; }
+__device__ inline int exp_of(double x) { int e; frexp(x, &e); return e; }
+__device__ inline float scale2(float x, int e) { return ldexpf(x, e); }
+__device__ inline double scale2(double x, int e) { return ldexp(x, e); }
+
+constexpr int PR_THREADS = 256;
+
+template <typename T, int TC>
+struct PruneSmem {
+    static constexpr int CPT = TC / 16;
+    static size_t bytes(int nslots, int nl, int nint)
+    {
+        size_t b = sizeof(T) * (2 * K2 + (size_t)nslots * K * TC);
+        b += sizeof(typename AtomMax<T>::U) * 2 * TC;
+        b += sizeof(int) * TC;
+        b += sizeof(SchedNode) * nint;
+        b = (b + 15) & ~size_t(15);
+        b += (size_t)nl * TC;
+        return (b + 15) & ~size_t(15);
+    }
+};
+
+template <typename T, int TC>
+__device__ inline void child_partial(const T *Et, const T *slots, int slot, int leaf, const uint8_t *lvT, int a0,
+                                     int c0, T v[4][TC / 16])
+{
+    constexpr int CPT = TC / 16;
+    if (slot < 0) {
+#pragma unroll
+        for (int cc = 0; cc < CPT; cc++) {
+            int s = lvT[leaf * TC + c0 + cc];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                int a = a0 + i;
+                v[i][cc] = (s >= K) ? (T)1 : (Et[s * K + a] + (a == s ? (T)1 : (T)0));
+            }
+        }
+        return;
+    }
+    const T *al = slots + (size_t)slot * K * TC;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        T x[CPT];
+        ColLoad<T, CPT>::load(al + (a0 + i) * TC + c0, x);
+#pragma unroll
+        for (int cc = 0; cc < CPT; cc++) v[i][cc] = x[cc];
+    }
+#pragma unroll 4
+    for (int j = 0; j < K; j++) {
+        T e[4], x[CPT];
+        Vec4<T>::load(Et + j * K + a0, e);
+        ColLoad<T, CPT>::load(al + j * TC + c0, x);
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int cc = 0; cc < CPT; cc++) v[i][cc] += e[i] * x[cc];
+    }
+}
+
+template <typename T, int TC>
+__global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
+{
+    constexpr int CPT = TC / 16;
+    typedef typename AtomMax<T>::U MU;
+    extern __shared__ __align__(16) unsigned char ssm[];
+    T *Et = reinterpret_cast<T *>(ssm);                 // [2][K][K]
+    T *slots = Et + 2 * K2;                              // [nslots][K][TC]
+    MU *colmax = reinterpret_cast<MU *>(slots + (size_t)a.nslots * K * TC);   // [2][TC]
+    int *cscale = reinterpret_cast<int *>(colmax + 2 * TC);                   // [TC]
+    SchedNode *sched = reinterpret_cast<SchedNode *>(cscale + TC);            // [n_internal]
+    size_t off = (reinterpret_cast<unsigned char *>(sched + a.n_internal) - ssm + 15) & ~size_t(15);
+    uint8_t *lvT = ssm + off;                                                  // [nl][TC]
+
+    const int tid = threadIdx.x;
+    const int ty = tid / 16, tx = tid % 16;
+    const int a0 = 4 * ty, c0 = CPT * tx;
+    const int nl = a.nl;
+    __shared__ double red_l[PR_THREADS / 32], red_e[PR_THREADS / 32];
+
+    for (int f = tid; f < a.n_internal; f += PR_THREADS) sched[f] = a.sched[f];
+
+    for (int w = blockIdx.x; w < a.nwi; w += gridDim.x) {
+        const WorkItem wi = a.wi[w];
+        const Request rq = a.req[wi.request];
+        const int md = rq.model;
+        const T *Pbase = reinterpret_cast<const T *>(a.Pbuf) + (size_t)rq.pset * a.nbr * K2;
+        const int ncols = wi.ncols;
+        const uint8_t *lg = a.leaves + (size_t)wi.col0 * nl;
+        __syncthreads();   // previous work item finished with shared memory
+        for (int f = tid; f < TC * nl; f += PR_THREADS) {
+            int c = f / nl, l = f - c * nl;
+            lvT[l * TC + c] = (c < ncols) ? lg[f] : (uint8_t)K;
+        }
+        for (int f = tid; f < 2 * TC; f += PR_THREADS) colmax[f] = 0;
+        for (int f = tid; f < TC; f += PR_THREADS) cscale[f] = 0;
+
+        for (int ni = 0; ni < a.n_internal; ni++) {
+            const SchedNode sn = sched[ni];
+            {
+                const float4 *gl = reinterpret_cast<const float4 *>(Pbase + (size_t)sn.lc * K2);
+                const float4 *gr = reinterpret_cast<const float4 *>(Pbase + (size_t)sn.rc * K2);
+                float4 *sl = reinterpret_cast<float4 *>(Et);
+                float4 *sr = reinterpret_cast<float4 *>(Et + K2);
+                constexpr int NV = K2 * sizeof(T) / 16;
+                for (int f = tid; f < NV; f += PR_THREADS) {
+                    sl[f] = __ldg(gl + f);
+                    sr[f] = __ldg(gr + f);
+                }
+            }
+            __syncthreads();
+            T vl[4][CPT], vr[4][CPT];
+            child_partial<T, TC>(Et, slots, sn.lslot, sn.lc, lvT, a0, c0, vl);
+            child_partial<T, TC>(Et + K2, slots, sn.rslot, sn.rc, lvT, a0, c0, vr);
+            __syncthreads();
+            MU *cm = colmax + (ni & 1) * TC;
+            MU *cm_next = colmax + ((ni + 1) & 1) * TC;
+            if (tid < TC) cm_next[tid] = 0;
+#pragma unroll
+            for (int cc = 0; cc < CPT; cc++) {
+                T mx = (T)0;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    vl[i][cc] *= vr[i][cc];
+                    mx = vl[i][cc] > mx ? vl[i][cc] : mx;
+                }
+                AtomMax<T>::upd(cm + c0 + cc, mx);
+            }
+            __syncthreads();
+            T *out = slots + (size_t)sn.oslot * K * TC;
+#pragma unroll
+            for (int cc = 0; cc < CPT; cc++) {
+                T mx = AtomMax<T>::get(cm + c0 + cc);
+                int e = (mx > (T)0) ? exp_of(mx) : 0;
+#pragma unroll
+                for (int i = 0; i < 4; i++) out[(a0 + i) * TC + c0 + cc] = scale2(vl[i][cc], -e);
+                if (ty == 0) cscale[c0 + cc] += e;
+            }
+        }
+        __syncthreads();
+        // root: z = alpha_root . prior ; elpr term = (alpha_root . prior*log prior) / z
+        double tl = 0.0, te = 0.0;
+        if (tid < TC && tid < ncols) {
+            const T *ar = slots + (size_t)sched[a.n_internal - 1].oslot * K * TC;
+            const double *pr = a.m.prior + md * K;
+            const double *wl = a.m.wlog + md * K;
+            double z = 0.0, wz = 0.0;
+            for (int s = 0; s < K; s++) {
+                double x = (double)ar[s * TC + tid];
+                z += x * pr[s];
+                wz += x * wl[s];
+            }
+            if (z > 0.0) {
+                tl = log(z) + (double)cscale[tid] * 0.69314718055994530942;
+                te = wz / z;
+            } else {
+                tl = -INFINITY;
+                te = 0.0;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            tl += __shfl_down_sync(0xffffffffu, tl, o);
+            te += __shfl_down_sync(0xffffffffu, te, o);
+        }
+        if ((tid & 31) == 0) { red_l[tid >> 5] = tl; red_e[tid >> 5] = te; }
+        __syncthreads();
+        if (tid == 0) {
+            double sl = 0.0, se = 0.0;
+            for (int k = 0; k < (TC + 31) / 32; k++) { sl += red_l[k]; se += red_e[k]; }
+            a.partials[2 * (size_t)w] = sl;
+            a.partials[2 * (size_t)w + 1] = se;
+        }
+    }
+}
+
+int prune_tile_cols(int prec)
+{
+    return prec == PCSF_PREC_FP64 ? 32 : 64;
+}
+
+size_t prune_smem_bytes(int prec, int nslots, int nl, int nint)
+{
+    if (prec == PCSF_PREC_FP64) return PruneSmem<double, 32>::bytes(nslots, nl, nint);
+    return PruneSmem<float, 64>::bytes(nslots, nl, nint);
+}
+
+template <typename T, int TC>
+static cudaError_t launch_prune_t(const PruneArgs &a, cudaStream_t s, int grid)
+{
+    size_t smem = PruneSmem<T, TC>::bytes(a.nslots, a.nl, a.n_internal);
+    cudaError_t e = cudaFuncSetAttribute(k_prune<T, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_prune<T, TC><<<grid, PR_THREADS, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prune(int prec, const PruneArgs &a, cudaStream_t s, int grid)
+{
+    if (a.nwi <= 0) return cudaSuccess;
+    if (prec == PCSF_PREC_FP64) return launch_prune_t<double, 32>(a, s, grid);
+    return launch_prune_t<float, 64>(a, s, grid);
+}
+
+// ---------------------------------------------------------------------------
+// Per-request sums of the work-item partials, in work-item order (deterministic).
+
+__global__ void k_reduce(const double *partials, const int32_t *wi_begin, int nreq, double *out_lpr, double *out_elpr)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nreq) return;
+    double sl = 0.0, se = 0.0;
+    for (int w = wi_begin[r]; w < wi_begin[r + 1]; w++) {
+        sl += partials[2 * (size_t)w];
+        se += partials[2 * (size_t)w + 1];
+    }
+    out_lpr[r] = sl;
+    out_elpr[r] = se;
+}
+
+cudaError_t launch_reduce(const double *partials, const int32_t *wi_begin, int nreq, double *out_lpr,
+                          double *out_elpr, cudaStream_t s)
+{
+    if (nreq <= 0) return cudaSuccess;
+    k_reduce<<<(nreq + 127) / 128, 128, 0, s>>>(partials, wi_begin, nreq, out_lpr, out_elpr);
+    return cudaGetLastError();
+}
+
+}  // namespace pcsf

@@ -1,0 +1,99 @@
+// Internal declarations shared by the host runtime and the CUDA kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/phylocsf_engine.h"
+
+namespace pcsf {
+
+constexpr int K = 64;          // codon states (Code.Codon64.dim)
+constexpr int K2 = K * K;
+constexpr int MAX_LEAVES = 512;
+
+// One internal node of the pruning schedule, in evaluation order.  A child
+// slot of -1 means the child is a leaf (its partial is a one-hot gather).
+struct SchedNode {
+    int16_t node, lc, rc;
+    int8_t lslot, rslot, oslot, pad;
+};
+static_assert(sizeof(SchedNode) == 10, "SchedNode layout");
+
+// A distinct (model, tree scale) pair: one set of P(t) matrices for every branch.
+struct PSet {
+    int32_t model;
+    int32_t pad;
+    double rho;
+};
+
+// A likelihood evaluation: region, model (0 coding / 1 noncoding), tree scale,
+// and the index of its P set within the launch chunk.
+struct Request {
+    int32_t region;
+    int32_t model;
+    int32_t pset;
+    int32_t pad;
+    double rho;
+};
+
+// A pruning work item: a tile of columns of one request's region.
+struct WorkItem {
+    int32_t request;   // index into the launch's request array
+    int32_t ncols;     // columns in this tile (<= tile width)
+    int64_t col0;      // first global column of the tile
+};
+
+// Device view of the two models' eigensystems (all arrays [2][...]).
+struct DevModels {
+    const double *U;        // [2][K][K]  eigenvectors of D^1/2 Q D^-1/2 (columns)
+    const float *Uf;        // [2][K][K]  FP32 copy
+    const double *lam;      // [2][K]
+    const double *sq;       // [2][K]     sqrt(pi)
+    const double *isq;      // [2][K]     1/sqrt(pi)
+    const double *wrow;     // [2][K]     w_m = sum_j U_jm sqrt(pi_j)  (row-sum identity)
+    const double *prior;    // [2][K]     root prior
+    const double *wlog;     // [2][K]     prior_a * log(prior_a)
+    double tol;             // Q.Diag tol (1e-6)
+};
+
+// Status keys: ((branch*K + row) << 4) | code, min-reduced so the first error
+// in the reference's (branch, row) order wins.  INT32_MAX = no error.
+constexpr int32_t STATUS_NONE = 0x7f7f7f7f;   // what cudaMemset(0x7f) leaves
+
+struct LaunchStats {
+    float ms = 0.f;
+};
+
+// ---- kernels (kernels.cu) -------------------------------------------------
+// Jacobi eigensolver: A [nmat][K][K] symmetric -> U [nmat][K][K], lam [nmat][K].
+cudaError_t launch_jacobi(const double *A, double *U, double *lam, int *status, int nmat, cudaStream_t s);
+
+// P(t) formation for P sets [nps]: writes E^T = (P - I)^T per branch into
+// Pbuf ([nps][nbr][K][K], element (j,i) = E[i][j]) in FP64 or FP32.
+cudaError_t launch_pform(bool fp64, const PSet *ps, int nps, const double *branch, int nbr,
+                         DevModels m, void *Pbuf, int32_t *status_key, cudaStream_t s);
+
+// Pruning over work items [nwi]; partials [nwi][2] (lpr, elpr).
+struct PruneArgs {
+    const WorkItem *wi;
+    int nwi;
+    const Request *req;
+    const uint8_t *leaves;   // [total_cols][nl]
+    const void *Pbuf;        // per chunk-local P set: [nbr][K][K] E^T
+    const SchedNode *sched;  // [n_internal]
+    int n_internal;
+    int nl;
+    int nbr;
+    int nslots;
+    DevModels m;
+    double *partials;        // [nwi][2]
+};
+cudaError_t launch_prune(int prec, const PruneArgs &a, cudaStream_t s, int grid);
+int prune_tile_cols(int prec);
+size_t prune_smem_bytes(int prec, int nslots, int nl, int nint);
+
+// Sum the partials of each request's contiguous work items in fixed order.
+cudaError_t launch_reduce(const double *partials, const int32_t *wi_begin, int nreq, double *out_lpr,
+                          double *out_elpr, cudaStream_t s);
+
+}  // namespace pcsf

@@ -1,0 +1,400 @@
+"""ctypes binding of the engine's C-ABI (include/phylocsf_engine.h, phylocsf_host.h).
+
+The Python surface mirrors the reference's model interface
+(src/PhyloCSFModel.ml): :func:`make` builds the coding/noncoding pair,
+:meth:`Engine.score` is ``PhyloCSFModel.score`` over many regions at once and
+:meth:`Engine.lpr` is ``lpr_leaves``.  There is no CPU fallback: without the
+compiled library or a GB300 every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _build
+
+PCSF_OK = 0
+STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory",
+                4: "CamlPaml.Q.substition_matrix: expm(tQ) entry < -tol",
+                5: "CamlPaml.Q.substitution matrix: row sum of expm(tQ) differs from 1",
+                6: "Assert_failure: renormalised diagonal of expm(tQ) not in (0,1]",
+                7: "Gsl.Error: endpoints do not enclose a minimum",
+                8: "eigensolver did not converge",
+                9: "CamlPaml.P14n.instantiate_q: Q scale evaluated to a non-positive value",
+                10: "capacity exceeded"}
+FIXED, MLE = 0, 1
+PREC = {"fp64": 0, "fp32": 1, "tf32x3": 2, "bf16x3": 3, "tf32": 4}
+MARGINALIZE = 64
+ORF_MODES = {"asis": 0, "atgstop": 1, "stopstop": 2, "stopstop3": 3, "tofirststop": 4,
+             "fromlaststop": 5, "toorfromstop": 6}
+
+
+class EngineError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("%s (status %d)" % (msg, status))
+        self.status = status
+
+
+class _Tree(ctypes.Structure):
+    _fields_ = [("n_leaves", ctypes.c_int32), ("parent", ctypes.POINTER(ctypes.c_int32)),
+                ("branch", ctypes.POINTER(ctypes.c_double))]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("score", ctypes.c_double), ("anc_comp_score", ctypes.c_double),
+                ("rho_c", ctypes.c_double), ("rho_n", ctypes.c_double),
+                ("lpr_c", ctypes.c_double), ("lpr_n", ctypes.c_double),
+                ("elpr_c", ctypes.c_double), ("elpr_n", ctypes.c_double),
+                ("status", ctypes.c_int32), ("evals", ctypes.c_int32)]
+
+
+RESULT_DTYPE = np.dtype([("score", "f8"), ("anc_comp_score", "f8"), ("rho_c", "f8"), ("rho_n", "f8"),
+                         ("lpr_c", "f8"), ("lpr_n", "f8"), ("elpr_c", "f8"), ("elpr_n", "f8"),
+                         ("status", "i4"), ("evals", "i4")])
+assert RESULT_DTYPE.itemsize == ctypes.sizeof(Result)
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("kernel_launches", ctypes.c_int64), ("evaluations", ctypes.c_int64),
+                ("column_branches", ctypes.c_int64), ("rounds", ctypes.c_int64),
+                ("prune_ms", ctypes.c_double), ("pform_ms", ctypes.c_double), ("other_ms", ctypes.c_double),
+                ("prune_launches", ctypes.c_int64), ("pform_launches", ctypes.c_int64)]
+
+
+# Every entry point declared in include/*.h, with its ctypes signature.
+_D = ctypes.POINTER(ctypes.c_double)
+_I32 = ctypes.POINTER(ctypes.c_int32)
+_I64 = ctypes.POINTER(ctypes.c_int64)
+_U8 = ctypes.POINTER(ctypes.c_uint8)
+_VP = ctypes.c_void_p
+SIGNATURES = {
+    "pcsf_engine_create": ([ctypes.POINTER(_Tree), _D, _D, _D, _D, ctypes.c_int32, ctypes.POINTER(_VP)], ctypes.c_int),
+    "pcsf_engine_create_q": ([ctypes.POINTER(_Tree), _D, _D, _D, _D, _D, _D, ctypes.c_int32, ctypes.POINTER(_VP)],
+                             ctypes.c_int),
+    "pcsf_engine_destroy": ([_VP], None),
+    "pcsf_last_error": ([_VP], ctypes.c_char_p),
+    "pcsf_engine_get_stats": ([_VP, ctypes.POINTER(Stats)], ctypes.c_int),
+    "pcsf_engine_reset_stats": ([_VP], ctypes.c_int),
+    "pcsf_engine_stream": ([_VP, ctypes.POINTER(_VP)], ctypes.c_int),
+    "pcsf_engine_eigensystem": ([_VP, ctypes.c_int32, _D, _D], ctypes.c_int),
+    "pcsf_engine_pt": ([_VP, ctypes.c_int32, ctypes.c_int32, _D, _D, _I32], ctypes.c_int),
+    "pcsf_batch_create": ([_VP, ctypes.c_int32, _I64, _U8, ctypes.POINTER(_VP)], ctypes.c_int),
+    "pcsf_batch_destroy": ([_VP], None),
+    "pcsf_score": ([_VP, _VP, ctypes.c_int32, ctypes.POINTER(Result)], ctypes.c_int),
+    "pcsf_score_batch": ([_VP, ctypes.c_int32, _I64, _U8, ctypes.c_int32, ctypes.POINTER(Result)], ctypes.c_int),
+    "pcsf_lpr": ([_VP, _VP, ctypes.c_int32, _D, _D, _D, _I32], ctypes.c_int),
+    "pcsf_grad": ([_VP, _VP, ctypes.c_int32, _D, _D, _D, _D, _I32], ctypes.c_int),
+    "pcsf_read_ecm": ([ctypes.c_char_p, _D, _D], ctypes.c_int),
+    "pcsf_parse_newick": ([ctypes.c_char_p, ctypes.c_int32, _I32, _I32, _D, ctypes.c_char_p, ctypes.c_int32],
+                          ctypes.c_int),
+    "pcsf_candidate_regions": ([ctypes.c_char_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                ctypes.c_int32, _I32, _I64, _I64, _I32], ctypes.c_int),
+    "pcsf_pack_regions": ([ctypes.c_int32, _I32, ctypes.c_int32, ctypes.POINTER(ctypes.c_char_p),
+                           ctypes.POINTER(ctypes.c_char_p), ctypes.c_int64, ctypes.c_int32, _I32, _I64, _I64, _I64,
+                           _U8], ctypes.c_int),
+    "pcsf_simulate": ([ctypes.c_int32, _I32, ctypes.c_int32, _D, _D, ctypes.c_int32, _I64, _I32, _D, ctypes.c_int32,
+                       ctypes.c_uint64, ctypes.c_int32, _U8], ctypes.c_int),
+}
+
+_LIB = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load_library(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load the in-tree library; raise if it is missing (no fallback exists)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError("phylocsf_gb300: native library %s is missing; run __graft_entry__.build()" % path)
+        _build.build()
+    lib = ctypes.CDLL(path)
+    for name, (args, res) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _LIB = lib
+    return lib
+
+
+def _p(a: np.ndarray, t):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def _err(lib, handle=None) -> str:
+    m = lib.pcsf_last_error(handle)
+    return m.decode() if m else ""
+
+
+def _check(rc: int, handle=None):
+    if rc != PCSF_OK:
+        lib = load_library()
+        raise EngineError(rc, _err(lib, handle) or STATUS_NAMES.get(rc, "error"))
+
+
+# --------------------------------------------------------------------------
+# host helpers
+
+
+class Tree:
+    """A tree in CamlPaml T order (leaves left to right, internal nodes post-order)."""
+
+    def __init__(self, parent: np.ndarray, branch: np.ndarray, labels: List[str]):
+        self.parent = np.ascontiguousarray(parent, np.int32)
+        self.branch = np.ascontiguousarray(branch, np.float64)   # [n] (root entry unused)
+        self.labels = labels
+        self.n = len(self.parent)
+        self.nl = (self.n + 1) // 2
+
+    @classmethod
+    def from_newick(cls, text: str) -> "Tree":
+        lib = load_library()
+        cap = 4096
+        nl = ctypes.c_int32()
+        parent = np.zeros(cap, np.int32)
+        branch = np.zeros(cap)
+        stride = 128
+        labels = ctypes.create_string_buffer(cap * stride)
+        _check(lib.pcsf_parse_newick(text.encode(), cap, ctypes.byref(nl), _p(parent, ctypes.c_int32),
+                                     _p(branch, ctypes.c_double), labels, stride))
+        n = 2 * nl.value - 1
+        raw = labels.raw
+        labs = [raw[i * stride:(i + 1) * stride].split(b"\0", 1)[0].decode() for i in range(n)]
+        return cls(parent[:n].copy(), branch[:n].copy(), labs)
+
+    @classmethod
+    def load(cls, path: str) -> "Tree":
+        with open(path) as f:
+            return cls.from_newick(f.read())
+
+    def scaled(self, factor: float) -> "Tree":
+        b = self.branch.copy()
+        b[: self.n - 1] *= factor
+        return Tree(self.parent.copy(), b, list(self.labels))
+
+    def c_struct(self) -> Tuple[_Tree, tuple]:
+        keep = (self.parent, np.ascontiguousarray(self.branch[: self.n - 1], np.float64))
+        return _Tree(self.nl, _p(keep[0], ctypes.c_int32), _p(keep[1], ctypes.c_double)), keep
+
+
+def read_ecm(path: str) -> Tuple[np.ndarray, np.ndarray]:
+    """ECM.import_parameters (src/ECM.ml:18-72) through the native reader."""
+    lib = load_library()
+    S = np.zeros((64, 64))
+    pi = np.zeros(64)
+    _check(lib.pcsf_read_ecm(path.encode(), _p(S, ctypes.c_double), _p(pi, ctypes.c_double)))
+    return S, pi
+
+
+def candidate_regions(ref: str, frames: int = 1, orf_mode: str = "AsIs", min_codons: int = 25):
+    lib = load_library()
+    mode = ORF_MODES[orf_mode.lower()]
+    cnt = ctypes.c_int32()
+    n = len(ref)
+    _check(lib.pcsf_candidate_regions(ref.encode(), n, frames, mode, min_codons, 0, None, None, None,
+                                      ctypes.byref(cnt)))
+    k = cnt.value
+    rc = np.zeros(max(k, 1), np.int32)
+    lo = np.zeros(max(k, 1), np.int64)
+    hi = np.zeros(max(k, 1), np.int64)
+    _check(lib.pcsf_candidate_regions(ref.encode(), n, frames, mode, min_codons, k, _p(rc, ctypes.c_int32),
+                                      _p(lo, ctypes.c_int64), _p(hi, ctypes.c_int64), ctypes.byref(cnt)))
+    return [(bool(rc[i]), int(lo[i]), int(hi[i])) for i in range(k)]
+
+
+def pack_regions(nl: int, leaf_rows: Sequence[Optional[int]], rows_fwd: Sequence[str], rows_rc: Sequence[str],
+                 regions: Sequence[Tuple[bool, int, int]]) -> Tuple[np.ndarray, np.ndarray]:
+    """pleaves over many regions: (col_offsets int64[R+1], leaves uint8[total, nl])."""
+    lib = load_library()
+    lr = np.array([-1 if r is None else r for r in leaf_rows], np.int32)
+    fw = (ctypes.c_char_p * len(rows_fwd))(*[s.encode() for s in rows_fwd])
+    rv = (ctypes.c_char_p * len(rows_rc))(*[s.encode() for s in rows_rc])
+    R = len(regions)
+    rc = np.array([1 if r[0] else 0 for r in regions] or [0], np.int32)
+    lo = np.array([r[1] for r in regions] or [0], np.int64)
+    hi = np.array([r[2] for r in regions] or [0], np.int64)
+    offs = np.zeros(R + 1, np.int64)
+    L = len(rows_fwd[0])
+    _check(lib.pcsf_pack_regions(nl, _p(lr, ctypes.c_int32), len(rows_fwd), fw, rv, L, R, _p(rc, ctypes.c_int32),
+                                 _p(lo, ctypes.c_int64), _p(hi, ctypes.c_int64), _p(offs, ctypes.c_int64), None))
+    leaves = np.zeros((int(offs[-1]), nl), np.uint8)
+    _check(lib.pcsf_pack_regions(nl, _p(lr, ctypes.c_int32), len(rows_fwd), fw, rv, L, R, _p(rc, ctypes.c_int32),
+                                 _p(lo, ctypes.c_int64), _p(hi, ctypes.c_int64), _p(offs, ctypes.c_int64),
+                                 _p(leaves, ctypes.c_uint8) if leaves.size else None))
+    return offs, leaves
+
+
+# --------------------------------------------------------------------------
+# engine
+
+
+class Batch:
+    """Regions resident in device memory (pcsf_batch)."""
+
+    def __init__(self, engine: "Engine", col_offsets: np.ndarray, leaves: np.ndarray):
+        self.engine = engine
+        lib = engine.lib
+        self.col_offsets = np.ascontiguousarray(col_offsets, np.int64)
+        self.n_regions = len(self.col_offsets) - 1
+        lv = np.ascontiguousarray(leaves, np.uint8)
+        if lv.ndim != 2 or lv.shape[1] != engine.nl:
+            raise ValueError("leaves must be [total_cols, n_leaves=%d]" % engine.nl)
+        self.total_cols = lv.shape[0]
+        h = _VP()
+        _check(lib.pcsf_batch_create(engine.handle, self.n_regions, _p(self.col_offsets, ctypes.c_int64),
+                                     _p(lv, ctypes.c_uint8), ctypes.byref(h)), engine.handle)
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.engine.lib.pcsf_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Engine:
+    """GB300 likelihood engine for one tree and a coding/noncoding model pair."""
+
+    def __init__(self, tree: Tree, S_c=None, pi_c=None, S_n=None, pi_n=None, precision: str = "fp32",
+                 Q=None, device: Optional[int] = None):
+        self.lib = load_library()
+        self.tree = tree
+        self.nl = tree.nl
+        self.precision = precision
+        flags = PREC[precision] | (0 if device is None else (device + 1) << 8)
+        ct, keep = tree.c_struct()
+        h = _VP()
+        if Q is None:
+            arrs = [np.ascontiguousarray(x, np.float64) for x in (S_c, pi_c, S_n, pi_n)]
+            rc = self.lib.pcsf_engine_create(ctypes.byref(ct), *[_p(a, ctypes.c_double) for a in arrs], flags,
+                                             ctypes.byref(h))
+        else:
+            arrs = [np.ascontiguousarray(x, np.float64) for x in Q]   # Qc, eqc, priorc, Qn, eqn, priorn
+            rc = self.lib.pcsf_engine_create_q(ctypes.byref(ct), *[_p(a, ctypes.c_double) for a in arrs], flags,
+                                               ctypes.byref(h))
+        _check(rc, None)
+        self.handle = h
+
+    @classmethod
+    def from_q(cls, tree: Tree, Q_c, eq_c, prior_c, Q_n, eq_n, prior_n, precision: str = "fp32",
+               device: Optional[int] = None) -> "Engine":
+        return cls(tree, precision=precision, Q=(Q_c, eq_c, prior_c, Q_n, eq_n, prior_n), device=device)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.pcsf_engine_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- data
+    def batch(self, col_offsets, leaves) -> Batch:
+        return Batch(self, col_offsets, leaves)
+
+    # ---- PhyloCSFModel.score over many regions
+    def score(self, batch: Batch, strategy: int = MLE) -> np.ndarray:
+        out = np.zeros(batch.n_regions, RESULT_DTYPE)
+        _check(self.lib.pcsf_score(self.handle, batch.handle, strategy,
+                                   out.ctypes.data_as(ctypes.POINTER(Result))), self.handle)
+        return out
+
+    def score_batch(self, col_offsets, leaves, strategy: int = MLE) -> np.ndarray:
+        """One-shot: host buffers in, results out (upload, score, free)."""
+        offs = np.ascontiguousarray(col_offsets, np.int64)
+        lv = np.ascontiguousarray(leaves, np.uint8)
+        out = np.zeros(len(offs) - 1, RESULT_DTYPE)
+        _check(self.lib.pcsf_score_batch(self.handle, len(offs) - 1, _p(offs, ctypes.c_int64),
+                                         _p(lv, ctypes.c_uint8), strategy,
+                                         out.ctypes.data_as(ctypes.POINTER(Result))), self.handle)
+        return out
+
+    # ---- lpr_leaves
+    def lpr(self, batch: Batch, model: int, rho) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
+        r = np.ascontiguousarray(np.broadcast_to(np.asarray(rho, np.float64), (batch.n_regions,)))
+        lpr = np.zeros(batch.n_regions)
+        elpr = np.zeros(batch.n_regions)
+        st = np.zeros(batch.n_regions, np.int32)
+        _check(self.lib.pcsf_lpr(self.handle, batch.handle, model, _p(r, ctypes.c_double),
+                                 _p(lpr, ctypes.c_double), _p(elpr, ctypes.c_double), _p(st, ctypes.c_int32)),
+               self.handle)
+        return lpr, elpr, st
+
+    def grad(self, batch: Batch, model: int, rho):
+        r = np.ascontiguousarray(np.broadcast_to(np.asarray(rho, np.float64), (batch.n_regions,)))
+        nbr = self.tree.n - 1
+        lpr = np.zeros(batch.n_regions)
+        db = np.zeros((batch.n_regions, nbr))
+        drho = np.zeros(batch.n_regions)
+        st = np.zeros(batch.n_regions, np.int32)
+        _check(self.lib.pcsf_grad(self.handle, batch.handle, model, _p(r, ctypes.c_double), _p(lpr, ctypes.c_double),
+                                  _p(db, ctypes.c_double), _p(drho, ctypes.c_double), _p(st, ctypes.c_int32)),
+               self.handle)
+        return lpr, db, drho, st
+
+    # ---- model introspection
+    def pt(self, model: int, t) -> Tuple[np.ndarray, np.ndarray]:
+        tt = np.ascontiguousarray(np.atleast_1d(np.asarray(t, np.float64)))
+        P = np.zeros((len(tt), 64, 64))
+        st = np.zeros(len(tt), np.int32)
+        _check(self.lib.pcsf_engine_pt(self.handle, model, len(tt), _p(tt, ctypes.c_double), _p(P, ctypes.c_double),
+                                       _p(st, ctypes.c_int32)), self.handle)
+        return P, st
+
+    def eigensystem(self, model: int) -> Tuple[np.ndarray, np.ndarray]:
+        U = np.zeros((64, 64))
+        lam = np.zeros(64)
+        _check(self.lib.pcsf_engine_eigensystem(self.handle, model, _p(U, ctypes.c_double), _p(lam, ctypes.c_double)),
+               self.handle)
+        return U, lam
+
+    def stats(self) -> dict:
+        s = Stats()
+        _check(self.lib.pcsf_engine_get_stats(self.handle, ctypes.byref(s)), self.handle)
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def stream_handle(self) -> int:
+        """The engine's cudaStream_t as an integer (for event timing on that stream)."""
+        h = _VP()
+        _check(self.lib.pcsf_engine_stream(self.handle, ctypes.byref(h)), self.handle)
+        return int(h.value or 0)
+
+    def reset_stats(self):
+        _check(self.lib.pcsf_engine_reset_stats(self.handle), self.handle)
+
+
+# --------------------------------------------------------------------------
+# PhyloCSFModel-style entry points
+
+
+def make(s1, pi1, s2, pi2, tree: Tree, precision: str = "fp32") -> Engine:
+    """PhyloCSFModel.make (PhyloCSFModel.ml:107-110): coding and noncoding models on one tree."""
+    return Engine(tree, s1, pi1, s2, pi2, precision=precision)
+
+
+def score(strategy: int, model: Engine, leaves: np.ndarray) -> np.void:
+    """PhyloCSFModel.score for one region's leaves ([ncols, nl] uint8)."""
+    lv = np.ascontiguousarray(leaves, np.uint8).reshape(-1, model.nl)
+    return model.score_batch(np.array([0, lv.shape[0]], np.int64), lv, strategy)[0]

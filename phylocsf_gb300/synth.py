@@ -1,0 +1,181 @@
+"""Seeded synthetic alignments for the benchmark and parity workloads.
+
+Columns are simulated along the tree as PhyloModel.simulate does
+(lib/CamlPaml/PhyloModel.ml:38-54: root ~ prior, child ~ P row of the parent
+state) with branch lengths at rho = 1, rejecting a stop codon in leaf 0 as
+testSim does (src/testSim.ml:52-65).  Gaps / N and entirely missing species
+are then marginalised per region.  The column simulation runs in the native
+helper ``pcsf_simulate`` (multithreaded, deterministic per column).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import engine as E
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+PARAMS_DIR = os.path.join(ROOT, "tests", "golden", "params")
+
+
+@dataclass
+class ParamSet:
+    name: str
+    tree: E.Tree
+    S_c: np.ndarray
+    pi_c: np.ndarray
+    S_n: np.ndarray
+    pi_n: np.ndarray
+
+
+def load_params(name: str, params_dir: Optional[str] = None) -> ParamSet:
+    """A parameter set (tree + coding/noncoding ECMs) from the committed fixtures."""
+    d = np.load(os.path.join(params_dir or PARAMS_DIR, name + ".npz"))
+
+    def full(tri):
+        S = np.zeros((64, 64))
+        il = np.tril_indices(64, -1)
+        S[il] = tri
+        return S + S.T
+
+    labels = [str(x) for x in d["labels"]]
+    tree = E.Tree(d["parent"].astype(np.int32), d["branch"].astype(np.float64), labels)
+    return ParamSet(name, tree, full(d["S_c"]), d["pi_c"].copy(), full(d["S_n"]), d["pi_n"].copy())
+
+
+def q_matrix(S: np.ndarray, pi: np.ndarray) -> np.ndarray:
+    """q_ij = s_ij pi_j, zero row sums, mean rate 1 (PhyloCSFModel.ml:11-30)."""
+    Q = S * pi[None, :]
+    np.fill_diagonal(Q, 0.0)
+    np.fill_diagonal(Q, -Q.sum(1))
+    return Q / (-(pi * np.diag(Q)).sum())
+
+
+def p_matrices(S: np.ndarray, pi: np.ndarray, t: np.ndarray) -> np.ndarray:
+    """P(t) for each t (numpy eigh of the symmetrised Q); rows clamped >= 0 and renormalised."""
+    Q = q_matrix(S, pi)
+    sq = np.sqrt(pi)
+    A = sq[:, None] * Q / sq[None, :]
+    lam, U = np.linalg.eigh(0.5 * (A + A.T))
+    out = np.empty((len(t), 64, 64))
+    for i, ti in enumerate(t):
+        M = (U * np.exp(lam * ti)) @ U.T
+        P = M * sq[None, :] / sq[:, None]
+        P = np.maximum(P, 0.0)
+        out[i] = P / P.sum(1, keepdims=True)
+    return out
+
+
+def simulate(ps: ParamSet, lengths: np.ndarray, models: np.ndarray, gap_frac: Optional[np.ndarray], seed: int,
+             reject_stop_leaf0: bool = True, threads: int = 0, rho: float = 1.0):
+    """Simulate regions: returns (col_offsets int64[R+1], leaves uint8[total, nl])."""
+    lib = E.load_library()
+    tree = ps.tree
+    nbr = tree.n - 1
+    t = tree.branch[:nbr] * rho
+    P = np.ascontiguousarray(np.stack([p_matrices(ps.S_c, ps.pi_c, t), p_matrices(ps.S_n, ps.pi_n, t)]))
+    prior = np.ascontiguousarray(np.stack([ps.pi_c, ps.pi_n]))
+    offs = np.zeros(len(lengths) + 1, np.int64)
+    offs[1:] = np.cumsum(lengths)
+    leaves = np.empty((int(offs[-1]), tree.nl), np.uint8)
+    models = np.ascontiguousarray(models, np.int32)
+    gf = None if gap_frac is None else np.ascontiguousarray(gap_frac, np.float64)
+    rc = lib.pcsf_simulate(tree.nl, E._p(tree.parent, ctypes.c_int32), 2, E._p(P, ctypes.c_double),
+                           E._p(prior, ctypes.c_double), len(lengths), E._p(offs, ctypes.c_int64),
+                           E._p(models, ctypes.c_int32), None if gf is None else E._p(gf, ctypes.c_double),
+                           1 if reject_stop_leaf0 else 0, seed, threads,
+                           E._p(leaves, ctypes.c_uint8) if leaves.size else E._p(np.zeros(1, np.uint8), ctypes.c_uint8))
+    E._check(rc)
+    return offs, leaves
+
+
+def gap_fractions(rng: np.random.Generator, nreg: int, nl: int, lo: float, hi: float, missing_max: float = 0.0):
+    """Per (region, species) gap probability ~ U(lo, hi); a U(0, missing_max)
+    fraction of each region's species (never leaf 0, the reference row) is
+    missing entirely (probability 1)."""
+    gf = rng.uniform(lo, hi, size=(nreg, nl))
+    if missing_max > 0:
+        for r in range(nreg):
+            k = int(round(rng.uniform(0.0, missing_max) * nl))
+            if k:
+                gone = rng.choice(np.arange(1, nl), size=min(k, nl - 1), replace=False)
+                gf[r, gone] = 1.0
+    return gf
+
+
+@dataclass
+class Workload:
+    name: str
+    params: ParamSet
+    col_offsets: np.ndarray
+    leaves: np.ndarray
+    models: np.ndarray
+    strategy: int
+
+    @property
+    def n_regions(self) -> int:
+        return len(self.col_offsets) - 1
+
+    @property
+    def total_cols(self) -> int:
+        return int(self.col_offsets[-1])
+
+
+def log_uniform_lengths(rng, n, lo, hi):
+    return np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi), size=n))).astype(np.int64).clip(lo, hi)
+
+
+def workload_12flies_fixed(seed: int = 0) -> Workload:
+    """One alignment of 300 codons on 12flies from the noncoding ECM, 10% gaps per species; fixed."""
+    ps = load_params("12flies")
+    rng = np.random.default_rng(seed)
+    gf = np.full((1, ps.tree.nl), 0.10)
+    offs, lv = simulate(ps, np.array([300]), np.array([1]), gf, seed)
+    del rng
+    return Workload("12flies_fixed_1x300", ps, offs, lv, np.array([1]), E.FIXED)
+
+
+def workload_58mammals_mle(n_regions: int = 10000, seed: int = 0) -> Workload:
+    """58mammals, mle: half coding / half noncoding, lengths log-uniform 50-3000 codons,
+    per-species gap+N fraction U(5%,40%), 0-20% of species entirely missing."""
+    ps = load_params("58mammals")
+    rng = np.random.default_rng(seed)
+    lengths = log_uniform_lengths(rng, n_regions, 50, 3000)
+    models = (np.arange(n_regions) % 2).astype(np.int32)    # 0 coding, 1 noncoding
+    gf = gap_fractions(rng, n_regions, ps.tree.nl, 0.05, 0.40, 0.20)
+    offs, lv = simulate(ps, lengths, models, gf, seed)
+    return Workload("58mammals_mle_%dregions" % n_regions, ps, offs, lv, models, E.MLE)
+
+
+def workload_120mammals_fixed(total_cols: int = 2_000_000, seed: int = 0) -> Workload:
+    """120mammals at rho = 1: alignments log-uniform 100-5000 codons totalling ~total_cols, 1:1 models."""
+    ps = load_params("120mammals")
+    rng = np.random.default_rng(seed)
+    lens = []
+    s = 0
+    while s < total_cols:
+        L = int(log_uniform_lengths(rng, 1, 100, 5000)[0])
+        L = min(L, total_cols - s) if total_cols - s >= 100 else L
+        lens.append(L)
+        s += L
+    lengths = np.array(lens, np.int64)
+    models = (np.arange(len(lengths)) % 2).astype(np.int32)
+    gf = gap_fractions(rng, len(lengths), ps.tree.nl, 0.05, 0.40, 0.0)
+    offs, lv = simulate(ps, lengths, models, gf, seed)
+    return Workload("120mammals_fixed_%dcols" % total_cols, ps, offs, lv, models, E.FIXED)
+
+
+def workload_100vertebrates_mle(n_regions: int = 20000, seed: int = 0) -> Workload:
+    """100vertebrates, mle: lengths log-uniform 30-10000 codons, coding:noncoding 1:3, 5-40% gaps."""
+    ps = load_params("100vertebrates")
+    rng = np.random.default_rng(seed)
+    lengths = log_uniform_lengths(rng, n_regions, 30, 10000)
+    models = (rng.random(n_regions) >= 0.25).astype(np.int32)
+    gf = gap_fractions(rng, n_regions, ps.tree.nl, 0.05, 0.40, 0.0)
+    offs, lv = simulate(ps, lengths, models, gf, seed)
+    return Workload("100vertebrates_mle_%dregions" % n_regions, ps, offs, lv, models, E.MLE)

@@ -1,0 +1,243 @@
+"""GPU parity: the CUDA engine (through the C-ABI) against the FP64 CPU oracle.
+
+Tolerances (stated per test):
+  - FP64 engine: P(t) entries within 1e-12, lpr within 1e-9 relative, scores
+    within 1e-6 dB (same Brent iterates as the oracle).
+  - FP32 engine (FP32 contractions on P-I, FP64 eigensystem / exp / sums):
+    P(t) entries within 2e-6, |d lpr| within 2.3e-4 nats (= 1e-3 dB) per
+    model on regions up to 3000 codons, fixed-strategy |d score| <= 1e-3 dB.
+"""
+import numpy as np
+import pytest
+
+import phylocsf_gb300 as P
+from phylocsf_gb300 import driver as D
+from phylocsf_gb300 import synth
+from oracle import oracle as O
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+DB_PER_NAT = 10.0 / np.log(10.0)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _oracle_fast():
+    O.set_sparse_leaves(True)
+
+
+_ENGINES = {}
+
+
+def engine(name, prec):
+    key = (name, prec)
+    if key not in _ENGINES:
+        ps = synth.load_params(name)
+        _ENGINES[key] = P.Engine(ps.tree, ps.S_c, ps.pi_c, ps.S_n, ps.pi_n, precision=prec)
+    return _ENGINES[key]
+
+
+PRECS = ["fp64", "fp32"]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_pt_matches_oracle(prec):
+    e = engine("58mammals", prec)
+    mc, mn, ot, tree = H.oracle_models("58mammals")
+    ts = np.array([0.0, 1e-4, 0.00655, 0.05, 0.3, 1.0, 4.0, 25.0])
+    tol = 1e-12 if prec == "fp64" else 2e-6
+    for m, om in ((0, mc), (1, mn)):
+        Pg, st = e.pt(m, ts)
+        assert (st == 0).all()
+        for i, t in enumerate(ts):
+            Po = om.pt(t)
+            assert np.abs(Pg[i] - Po).max() <= tol, (m, t, np.abs(Pg[i] - Po).max())
+            assert np.allclose(Pg[i].sum(1), 1.0, atol=tol * 64)
+            assert (Pg[i] >= 0).all()
+
+
+def test_eigensystem_matches_oracle():
+    e = engine("12flies", "fp64")
+    mc, mn, ot, tree = H.oracle_models("12flies")
+    for m, om in ((0, mc), (1, mn)):
+        U, lam = e.eigensystem(m)
+        assert np.allclose(np.sort(lam), np.sort(om.lam), atol=1e-12)
+        assert np.allclose(U.T @ U, np.eye(64), atol=1e-12)
+
+
+def _synthetic(name, lengths, seed, gaps=(0.05, 0.4), missing=0.2):
+    ps = synth.load_params(name)
+    rng = np.random.default_rng(seed)
+    lengths = np.asarray(lengths, np.int64)
+    models = (np.arange(len(lengths)) % 2).astype(np.int32)
+    gf = synth.gap_fractions(rng, len(lengths), ps.tree.nl, gaps[0], gaps[1], missing)
+    return synth.simulate(ps, lengths, models, gf, seed)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("name,lengths", [("12flies", [300, 1, 64, 65, 129, 0, 7]),
+                                          ("58mammals", [50, 333, 1000, 3000])])
+def test_lpr_matches_oracle(prec, name, lengths):
+    e = engine(name, prec)
+    mc, mn, ot, tree = H.oracle_models(name)
+    offs, leaves = _synthetic(name, lengths, seed=11)
+    b = e.batch(offs, leaves)
+    for model, om in ((0, mc), (1, mn)):
+        for rho in (0.01, 0.37, 1.0, 3.3, 10.0):
+            lpr, elpr, st = e.lpr(b, model, rho)
+            assert (st == 0).all()
+            for r in range(len(lengths)):
+                lv = H.u8_to_oracle(leaves[offs[r]:offs[r + 1]])
+                lo, eo = O.lpr_leaves(om, ot, rho, lv)
+                if prec == "fp64":
+                    assert lpr[r] == pytest.approx(lo, rel=1e-9, abs=1e-9)
+                    assert elpr[r] == pytest.approx(eo, rel=1e-9, abs=1e-9)
+                else:
+                    assert abs(lpr[r] - lo) <= 2.3e-4, (r, rho, lpr[r] - lo)
+                    assert abs(elpr[r] - eo) <= 2.3e-4, (r, rho, elpr[r] - eo)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_fixed_scores_match_oracle_fixtures(prec):
+    for fa, rec in H.oracle_fixed().items():
+        e = engine(rec["params"], prec)
+        ex = H.examples()[fa]
+        res = D.process_alignment(e, _mfa(ex), D.Options(strategy=P.FIXED, anc_comp=True))
+        r = res.best.result
+        tol = 1e-6 if prec == "fp64" else 1e-3
+        assert abs(r["score"] - rec["score"]) <= tol
+        assert abs(r["anc_comp_score"] - rec["anc"]) <= tol
+
+
+def _mfa(ex):
+    return "\n".join(">%s\n%s" % (s, r) for s, r in zip(ex["species"], ex["rows"])) + "\n"
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("idx", [0, 1, 2, 3])
+def test_reference_pins_through_gpu(prec, idx):
+    """src/test.ml:27-59 through the GPU driver path (mle)."""
+    p = H.pins()[idx]
+    f = H.parse_flags(p["flags"])
+    e = engine(p["params"], prec)
+    ex = H.examples()[p["file"]]
+    opts = D.Options(strategy=P.MLE, frames=f["frames"], orf_mode=f["orf"], remove_ref_gaps=f["remove_ref_gaps"],
+                     anc_comp=True, aa=f["aa"])
+    res = D.process_alignment(e, _mfa(ex), opts, fn=p["file"])
+    best = res.best
+    wins = p["windows"]
+    assert wins[0][0] < best.result["score"] < wins[0][1], best.result["score"]
+    if len(wins) > 1:
+        assert wins[1][0] < best.result["anc_comp_score"] < wins[1][1]
+    if p["ints"]:
+        assert [best.lo, best.hi] == p["ints"]
+    if p["strand"]:
+        assert (not best.rc) == (p["strand"] == "+")
+    if f["aa"]:
+        assert res.lines[-1].split("\t")[-1].startswith("MLRAALTTVRRGPRLSRLLSAAA")
+
+
+def test_mle_fp64_follows_oracle_iterates():
+    e = engine("29mammals", "fp64")
+    mc, mn, ot, tree = H.oracle_models("29mammals")
+    offs, leaves = _synthetic("29mammals", [40, 120, 200, 75, 1], seed=5)
+    res = e.score_batch(offs, leaves, P.MLE)
+    for r in range(len(offs) - 1):
+        lv = H.u8_to_oracle(leaves[offs[r]:offs[r + 1]])
+        o = O.score_region(mc, mn, ot, O.MLE, lv)
+        g = res[r]
+        assert g["status"] == 0 and o.status == 0
+        assert abs(g["score"] - o.score) <= 1e-6
+        assert abs(g["anc_comp_score"] - o.anc) <= 1e-6
+        assert g["rho_c"] == pytest.approx(o.rho_c, rel=1e-9)
+        assert g["rho_n"] == pytest.approx(o.rho_n, rel=1e-9)
+
+
+def test_mle_fp32_close_to_fp64():
+    """The split-free FP32 path against the FP64 path on mle scores (Brent included)."""
+    offs, leaves = _synthetic("58mammals", list(np.random.default_rng(2).integers(50, 1500, size=64)), seed=2)
+    a = engine("58mammals", "fp64").score_batch(offs, leaves, P.MLE)
+    b = engine("58mammals", "fp32").score_batch(offs, leaves, P.MLE)
+    assert (a["status"] == 0).all() and (b["status"] == 0).all()
+    d = np.abs(a["score"] - b["score"])
+    assert np.median(d) <= 1e-3
+    assert (d <= 1e-3).mean() >= 0.95, np.sort(d)[-8:]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_beagle_tinytest_embedded(prec):
+    """lib/CamlPaml/test.ml:56-99 with the 4-state JC69 model embedded in the 64 codon states
+    (states 4..63 have no rate and a negligible root prior)."""
+    b = H.beagle()
+    tree = P.Tree.from_newick(b["tree"])
+    Q = np.zeros((64, 64))
+    Q[:4, :4] = 1.0 / 3.0
+    np.fill_diagonal(Q[:4, :4], -1.0)
+    eq = np.ones(64)
+    eq[:4] = 0.25
+    prior = np.full(64, 1e-300)
+    prior[:4] = 0.25
+    e = P.Engine.from_q(tree, Q, eq, prior, Q, eq, prior, precision=prec)
+    seqs = b["seqs"]
+    order = [seqs[tree.labels[i]] for i in range(tree.nl)]
+    L = len(order[0])
+    lv = np.array([[("ACGT".index(s[i]) if s[i] in "ACGT" else 64) for s in order] for i in range(L)], np.uint8)
+    bt = e.batch(np.array([0, L], np.int64), lv)
+    lpr, _, st = e.lpr(bt, 0, 1.0)
+    assert st[0] == 0
+    assert abs(lpr[0] - b["logL"]) <= b["eps"]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_edge_cases(prec):
+    e = engine("12flies", prec)
+    mc, mn, ot, tree = H.oracle_models("12flies")
+    nl = tree.nl
+    cols = [np.full((0, nl), 64, np.uint8),                   # empty region
+            np.full((5, nl), 64, np.uint8),                   # all marginalised
+            np.array([[0] * nl], np.uint8),                   # one column, all AAA
+            np.tile(np.arange(nl, dtype=np.uint8) + 40, (64, 1))]   # exactly one tile
+    offs = np.zeros(len(cols) + 1, np.int64)
+    offs[1:] = np.cumsum([c.shape[0] for c in cols])
+    leaves = np.concatenate(cols)
+    res = e.score_batch(offs, leaves, P.MLE)
+    assert (res["status"] == 0).all()
+    assert res[0]["score"] == 0.0 and res[0]["rho_c"] == 10.0       # find_init exhausts its tries
+    for r in range(1, len(cols)):
+        lv = H.u8_to_oracle(cols[r])
+        o = O.score_region(mc, mn, ot, O.MLE, lv)
+        assert abs(res[r]["score"] - o.score) <= (1e-6 if prec == "fp64" else 1e-3)
+    with pytest.raises(P.EngineError):
+        e.batch(np.array([0, 1], np.int64), np.full((1, nl), 65, np.uint8))     # invalid leaf code
+    with pytest.raises(P.EngineError):
+        e.batch(np.array([0, 2, 1], np.int64), np.zeros((2, nl), np.uint8))     # decreasing offsets
+
+
+def test_deterministic():
+    e = engine("58mammals", "fp32")
+    offs, leaves = _synthetic("58mammals", [500, 70, 1200], seed=9)
+    a = e.score_batch(offs, leaves, P.MLE)
+    b = e.score_batch(offs, leaves, P.MLE)
+    assert a.tobytes() == b.tobytes()
+
+
+def test_region_order_invariance():
+    e = engine("58mammals", "fp32")
+    offs, leaves = _synthetic("58mammals", [300, 80, 700, 64], seed=4)
+    a = e.score_batch(offs, leaves, P.FIXED)
+    perm = [2, 0, 3, 1]
+    parts = [leaves[offs[i]:offs[i + 1]] for i in perm]
+    offs2 = np.zeros(5, np.int64)
+    offs2[1:] = np.cumsum([p.shape[0] for p in parts])
+    b = e.score_batch(offs2, np.concatenate(parts), P.FIXED)
+    assert np.array_equal(a["score"][perm], b["score"])
+
+
+def test_stats_count_kernels():
+    e = engine("12flies", "fp32")
+    e.reset_stats()
+    offs, leaves = _synthetic("12flies", [100, 200], seed=1)
+    e.score_batch(offs, leaves, P.FIXED)
+    s = e.stats()
+    assert s["kernel_launches"] >= 3 and s["evaluations"] == 4
+    assert s["column_branches"] == 300 * 2 * (2 * 12 - 2)
