@@ -168,7 +168,8 @@ def run_reference(args, world, rank):
     line = {"metric": METRIC, "value": v, "unit": "regions/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * total / max(step, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": wl.name, "strategy": "mle", "tree": "58mammals", "regions": wl.n_regions},
+            "config": {"workload": wl.name, "strategy": "mle" if wl.strategy else "fixed", "tree": wl.params.name,
+                       "regions": wl.n_regions},
             "cpu_baseline": {"value": v, "unit": "regions/s", "cores": cores, "kind": "port",
                              "sample": "%d random regions per step of the workload, one process per core, "
                                        "FP64 oracle with the reference's dense loop" % cores},
@@ -279,7 +280,7 @@ def run_ours(args, world, rank, local):
 
     line = {"metric": METRIC, "value": value, "unit": "regions/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": {"fp32": "f32", "fp64": "f64"}.get(args.precision, args.precision),
+            "vs_baseline": None, "dtype": {"fp32": "f32", "fp32c": "f32 (compensated)", "fp64": "f64"}.get(args.precision, args.precision),
             "data": "synthetic (seeded simulation along the tree; no public benchmark exists)",
             "config": {"workload": wl.name, "tree": ps.name, "strategy": "mle" if wl.strategy else "fixed",
                        "regions_per_gpu": wl.n_regions, "columns_per_gpu": wl.total_cols,
@@ -343,7 +344,7 @@ def main():
     ap.add_argument("--workload", default="58mammals_mle")
     ap.add_argument("--regions", type=int, default=10000)
     ap.add_argument("--cols", type=int, default=2_000_000)
-    ap.add_argument("--precision", default="fp32")
+    ap.add_argument("--precision", default="fp32c")
     ap.add_argument("--fp64-regions", type=int, default=256)
     ap.add_argument("--cpu-cores", type=int, default=0)
     ap.add_argument("--no-accuracy", action="store_true")

@@ -54,6 +54,11 @@ extern "C" {
 #define PCSF_PREC_BF16X3 3 /* tcgen05 BF16 hi/lo split (3 products), FP32 accumulate */
 #define PCSF_PREC_TF32 4  /* tcgen05 single TF32 product (precision study only)      */
 
+/* engine flag: compensated (Kahan) summation in the FP32 contractions.  FP32
+ * accumulation of many small positive terms into a large sum drops the ones
+ * below half an ulp, a bias that accumulates over thousands of columns. */
+#define PCSF_COMPENSATED (1 << 16)
+
 /* engine flags, bits 8..15: CUDA device ordinal + 1 (0 = the calling thread's
  * current device).  Every call on an engine runs on the engine's device. */
 #define PCSF_DEVICE(d) ((((int32_t)(d)) + 1) << 8)

@@ -19,6 +19,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -98,6 +99,7 @@ struct pcsf_engine {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[8] = {};
     int prec = PCSF_PREC_FP32;
+    bool compensated = false;
     std::string err;
 
     // tree
@@ -114,7 +116,8 @@ struct pcsf_engine {
 
     // device copies
     DevBuf<double> dU, dlam, dsq, disq, dwrow, dprior, dwlog, dbranch;
-    DevBuf<float> dUf;
+    DevBuf<float> dUf, dgridT, dQf, dQ2f;
+    DevBuf<double> dgrid_t;
     DevBuf<SchedNode> dsched;
     DevModels dm{};
 
@@ -277,6 +280,60 @@ static int assemble_q(const double *S, const double *pi, double *Q)
     return PCSF_OK;
 }
 
+// FP32 P(t) formation support: E(t_g) = P(t_g) - I on a geometric grid
+// t_g = t0 r^g (t0 = 1e-5, r = 1.01) formed in FP64 and stored in FP32, plus
+// Q and Q^2 for t < t0.  A branch then needs only the FP32 correction
+// D^-1/2 U diag(e^{lam t} - e^{lam t_g}) U^T D^1/2, whose rounding error is
+// proportional to |t - t_g| <= 0.5% of t instead of t itself.
+static int build_pt_grid(pcsf_engine *e, const double *Q[2])
+{
+    const double t0 = 1e-5, ratio = 1.01;
+    double bmax = 0.0;
+    for (double b : e->branch) bmax = std::max(bmax, b);
+    const double tmax = std::max(10.5 * bmax, 1.0);
+    const double lr = std::log(ratio);
+    const int G = (int)std::ceil(std::log(tmax / t0) / lr) + 1;
+    std::vector<double> gt(G);
+    for (int g = 0; g < G; g++) gt[g] = t0 * std::exp(g * lr);
+    CK(e->dgrid_t.reserve(G), "cudaMalloc");
+    CK(e->dgridT.reserve((size_t)2 * G * K2), "cudaMalloc");
+    CK(cudaMemcpyAsync(e->dgrid_t.p, gt.data(), sizeof(double) * G, cudaMemcpyHostToDevice, e->stream), "H2D grid");
+    DevBuf<double> tmp;
+    DevBuf<PSet> dps;
+    DevBuf<int32_t> dst;
+    CK(tmp.reserve((size_t)G * K2), "cudaMalloc");
+    CK(dps.reserve(2), "cudaMalloc");
+    CK(dst.reserve(2), "cudaMalloc");
+    PSet ps[2] = {{0, 0, 1.0}, {1, 0, 1.0}};
+    CK(cudaMemcpyAsync(dps.p, ps, sizeof ps, cudaMemcpyHostToDevice, e->stream), "H2D");
+    for (int m = 0; m < 2; m++) {
+        CK(launch_pform(true, dps.p + m, 1, e->dgrid_t.p, G, e->dm, tmp.p, dst.p + m, e->stream, true), "grid launch");
+        CK(launch_d2f(tmp.p, e->dgridT.p + (size_t)m * G * K2, (size_t)G * K2, e->stream), "grid convert");
+        e->stats.kernel_launches += 2;
+    }
+    std::vector<float> qf(2 * K2), q2f(2 * K2);
+    for (int m = 0; m < 2; m++)
+        for (int i = 0; i < K; i++)
+            for (int j = 0; j < K; j++) {
+                double acc = 0.0;
+                for (int k = 0; k < K; k++) acc += Q[m][i * K + k] * Q[m][k * K + j];
+                qf[m * K2 + i * K + j] = (float)Q[m][i * K + j];
+                q2f[m * K2 + i * K + j] = (float)acc;
+            }
+    CK(e->dQf.reserve(2 * K2), "cudaMalloc");
+    CK(e->dQ2f.reserve(2 * K2), "cudaMalloc");
+    CK(cudaMemcpyAsync(e->dQf.p, qf.data(), sizeof(float) * 2 * K2, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(e->dQ2f.p, q2f.data(), sizeof(float) * 2 * K2, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaStreamSynchronize(e->stream), "P(t) grid");
+    e->dm.gridT = e->dgridT.p;
+    e->dm.grid_t = e->dgrid_t.p;
+    e->dm.grid_n = G;
+    e->dm.grid_lr = lr;
+    e->dm.Qf = e->dQf.p;
+    e->dm.Q2f = e->dQ2f.p;
+    return PCSF_OK;
+}
+
 static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2], const double *prior[2])
 {
     // symmetric similarity transforms A = D^1/2 Q D^-1/2, eigendecomposed in FP64 on the device
@@ -354,6 +411,11 @@ static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2],
     e->dm.prior = e->dprior.p;
     e->dm.wlog = e->dwlog.p;
     e->dm.tol = e->tol;
+    e->dm.grid_n = 0;
+    if (e->prec != PCSF_PREC_FP64) {
+        int rc = build_pt_grid(e, Q);
+        if (rc) return rc;
+    }
     return PCSF_OK;
 }
 
@@ -363,6 +425,7 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
     if (prec != PCSF_PREC_FP64 && prec != PCSF_PREC_FP32)
         return e->fail(PCSF_EINVAL, "precision mode %d is not available in this build", prec);
     e->prec = prec;
+    e->compensated = (flags & PCSF_COMPENSATED) != 0;
     int ndev = 0;
     cudaError_t ce = cudaGetDeviceCount(&ndev);
     if (ce != cudaSuccess || ndev == 0)
@@ -518,7 +581,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         pa.m = e->dm;
         pa.partials = e->dpart.p + 2 * (size_t)wib[r0];
         int grid = std::min(e->prune_grid, std::max(pa.nwi, 1));
-        CK(launch_prune(e->prec, pa, s, grid), "pruning launch");
+        CK(launch_prune(e->prec, e->compensated, pa, s, grid), "pruning launch");
         CK(cudaEventRecord(e->ev[2], s), "event");
         e->stats.pform_launches += (p1 > p0);
         e->stats.prune_launches += (pa.nwi > 0);
@@ -758,6 +821,9 @@ static double decibans(double x) { return 10.0 * x / std::log(10.0); }
 
 static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
 {
+    // PCSF_TRACE_REGION=<r>: print every evaluation of region r's fits to stderr
+    const char *tr = std::getenv("PCSF_TRACE_REGION");
+    const int trace = tr ? std::atoi(tr) : -1;
     std::vector<Request> reqs;
     std::vector<std::pair<int, double>> owner;
     std::vector<Eval> res;
@@ -787,7 +853,14 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
         e->stats.rounds += 1;
         int rc = evaluate(e, b, reqs, res);
         if (rc) return rc;
-        for (size_t k = 0; k < reqs.size(); k++) fits[owner[k].first].cache.push_back({owner[k].second, res[k]});
+        for (size_t k = 0; k < reqs.size(); k++) {
+            Fit &f = fits[owner[k].first];
+            f.cache.push_back({owner[k].second, res[k]});
+            if (f.region == trace)
+                std::fprintf(stderr, "trace region %d model %d round %lld rho %.17g lpr %.17g status %d | phase %d bx %.17g [%.17g %.17g]\n",
+                             f.region, f.model, (long long)e->stats.rounds, owner[k].second, res[k].lpr, res[k].status,
+                             (int)f.phase, f.bx, f.blo, f.bhi);
+        }
     }
     return PCSF_OK;
 }

@@ -181,15 +181,17 @@ __device__ inline void status_min(int32_t *key, int branch, int row, int code)
 
 template <typename T>
 __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const double *branch, int nbr,
-                                                       DevModels m, T *Pbuf, int32_t *status_key)
+                                                       DevModels m, T *Pbuf, int32_t *status_key, int raw)
 {
     extern __shared__ __align__(16) unsigned char psm[];
     T *UT = reinterpret_cast<T *>(psm);     // [K][K]   UT[m][j] = U[j][m]
-    T *UeT = UT + K2;                         // [K][K]   UeT[m][i] = U[i][m] * expm1(lam_m t)
+    T *UeT = UT + K2;                         // [K][K]   UeT[m][i] = U[i][m] * coef_m
     T *Es = UeT + K2;                         // [K][K+1] E[i][j]
     T *sqT = Es + K * (K + 1);                // [K]
     T *isqT = sqT + K;                        // [K]
-    double *ex = reinterpret_cast<double *>(isqT + K);   // [K]
+    double *ex = reinterpret_cast<double *>(isqT + K);   // [K] expm1(lam t): row-sum identity
+    double *cf = ex + K;                                 // [K] GEMM coefficients
+    __shared__ int mode_s, grid_s;
     const int tid = threadIdx.x;
     const int r = blockIdx.y;
     const PSet rq = ps[r];
@@ -199,10 +201,11 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
     const double *lam = m.lam + md * K;
     const double *isq = m.isq + md * K;
     const double *wrow = m.wrow + md * K;
+    const bool fp32 = sizeof(T) == 4;
 
     for (int f = tid; f < K2; f += PF_THREADS) {
         int j = f / K, mm = f % K;   // U[j][mm]
-        UT[mm * K + j] = (sizeof(T) == 8) ? (T)U[f] : (T)Uf[f];
+        UT[mm * K + j] = fp32 ? (T)Uf[f] : (T)U[f];
     }
     if (tid < K) {
         sqT[tid] = (T)m.sq[md * K + tid];
@@ -214,36 +217,76 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
         if (b >= nbr) break;                       // uniform across the block
         const double t = rq.rho * branch[b];
         __syncthreads();                           // UT ready / previous branch done with smem
-        if (tid < K) ex[tid] = expm1(lam[tid] * t);
-        __syncthreads();
-        for (int f = tid; f < K2; f += PF_THREADS) {
-            int mm = f / K;
-            UeT[f] = UT[f] * (T)ex[mm];
+        if (tid == 0) {
+            // 0: direct eigen formula (FP64);  1: t == 0;  2: Taylor below the grid;  3: grid correction
+            int mode = 0, g = 0;
+            if (fp32 && m.grid_n > 0) {
+                if (t == 0.0) mode = 1;
+                else if (t < m.grid_t[0]) mode = 2;
+                else {
+                    mode = 3;
+                    double x = log(t / m.grid_t[0]) / m.grid_lr;
+                    g = (int)floor(x);
+                    if (g < 0) g = 0;
+                    if (g > m.grid_n - 1) g = m.grid_n - 1;
+                    if (g + 1 < m.grid_n && (m.grid_t[g + 1] - t) < (t - m.grid_t[g])) g++;
+                }
+            }
+            mode_s = mode;
+            grid_s = g;
         }
         __syncthreads();
-        T acc[4][4];
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-#pragma unroll
-            for (int j = 0; j < 4; j++) acc[i][j] = (T)0;
-        for (int mm = 0; mm < K; mm++) {
-            T a[4], bb[4];
-            Vec4<T>::load(UeT + mm * K + 4 * ty, a);
-            Vec4<T>::load(UT + mm * K + 4 * tx, bb);
+        const int mode = mode_s;
+        if (tid < K) {
+            ex[tid] = expm1(lam[tid] * t);
+            if (mode == 3) {
+                const double tg = m.grid_t[grid_s];
+                cf[tid] = exp(lam[tid] * tg) * expm1(lam[tid] * (t - tg));
+            } else {
+                cf[tid] = ex[tid];
+            }
+        }
+        __syncthreads();
+        if (mode == 0 || mode == 3) {
+            for (int f = tid; f < K2; f += PF_THREADS) {
+                int mm = f / K;
+                UeT[f] = UT[f] * (T)cf[mm];
+            }
+            __syncthreads();
+            T acc[4][4];
 #pragma unroll
             for (int i = 0; i < 4; i++)
 #pragma unroll
-                for (int j = 0; j < 4; j++) acc[i][j] += a[i] * bb[j];
-        }
+                for (int j = 0; j < 4; j++) acc[i][j] = (T)0;
+            for (int mm = 0; mm < K; mm++) {
+                T a[4], bb[4];
+                Vec4<T>::load(UeT + mm * K + 4 * ty, a);
+                Vec4<T>::load(UT + mm * K + 4 * tx, bb);
 #pragma unroll
-        for (int i = 0; i < 4; i++)
+                for (int i = 0; i < 4; i++)
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                int ii = 4 * ty + i, jj = 4 * tx + j;
-                Es[ii * (K + 1) + jj] = acc[i][j] * sqT[jj] * isqT[ii];
+                    for (int j = 0; j < 4; j++) acc[i][j] += a[i] * bb[j];
             }
+            const float *base = (mode == 3) ? m.gridT + ((size_t)md * m.grid_n + grid_s) * K2 : nullptr;
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    int ii = 4 * ty + i, jj = 4 * tx + j;
+                    T v = acc[i][j] * sqT[jj] * isqT[ii];
+                    if (base) v += (T)base[jj * K + ii];
+                    Es[ii * (K + 1) + jj] = v;
+                }
+        } else {
+            const float *Qf = m.Qf + (size_t)md * K2, *Q2f = m.Q2f + (size_t)md * K2;
+            const T tt = (T)t, h = (T)(0.5 * t * t);
+            for (int f = tid; f < K2; f += PF_THREADS) {
+                int i = f / K, j = f % K;
+                Es[i * (K + 1) + j] = (mode == 1) ? (T)0 : tt * (T)Qf[f] + h * (T)Q2f[f];
+            }
+        }
         __syncthreads();
-        if (tid < K) {
+        if (tid < K && !raw) {
             const int i = tid;
             // raw row sum - 1, in FP64 through the eigensystem
             double rs = 0.0;
@@ -282,22 +325,35 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
 }
 
 cudaError_t launch_pform(bool fp64, const PSet *req, int nreq, const double *branch, int nbr, DevModels m,
-                         void *Pbuf, int32_t *status_key, cudaStream_t s)
+                         void *Pbuf, int32_t *status_key, cudaStream_t s, bool raw)
 {
     if (nreq <= 0) return cudaSuccess;
     dim3 grid((nbr + PF_BRANCHES - 1) / PF_BRANCHES, nreq);
     if (fp64) {
-        size_t smem = sizeof(double) * (2 * K2 + K * (K + 1) + 3 * K);
+        size_t smem = sizeof(double) * (2 * K2 + K * (K + 1) + 4 * K);
         cudaError_t e = cudaFuncSetAttribute(k_pform<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k_pform<double><<<grid, PF_THREADS, smem, s>>>(req, branch, nbr, m, (double *)Pbuf, status_key);
+        k_pform<double><<<grid, PF_THREADS, smem, s>>>(req, branch, nbr, m, (double *)Pbuf, status_key, raw ? 1 : 0);
     } else {
-        size_t smem = sizeof(float) * (2 * K2 + K * (K + 1) + 2 * K) + sizeof(double) * K;
+        size_t smem = sizeof(float) * (2 * K2 + K * (K + 1) + 2 * K);
         smem = (smem + 15) & ~size_t(15);
+        smem += sizeof(double) * 2 * K;
         cudaError_t e = cudaFuncSetAttribute(k_pform<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k_pform<float><<<grid, PF_THREADS, smem, s>>>(req, branch, nbr, m, (float *)Pbuf, status_key);
+        k_pform<float><<<grid, PF_THREADS, smem, s>>>(req, branch, nbr, m, (float *)Pbuf, status_key, raw ? 1 : 0);
     }
+    return cudaGetLastError();
+}
+
+__global__ void k_d2f(const double *in, float *out, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
+cudaError_t launch_d2f(const double *in, float *out, size_t n, cudaStream_t s)
+{
+    k_d2f<<<264, 256, 0, s>>>(in, out, n);
     return cudaGetLastError();
 }
 
@@ -309,7 +365,8 @@ cudaError_t launch_pform(bool fp64, const PSet *req, int nreq, const double *bra
 // tx*CPT..tx*CPT+CPT-1.
 //
 // For a child c of node i:   v_c[a] = alpha_c[a] + sum_j E_c[a][j] alpha_c[j]
-// (internal child; E = P - I keeps the large diagonal exact), or the gather
+// (internal child; E = P - I keeps the large diagonal exact; the sum is formed
+// first, optionally with compensated summation, and alpha_c[a] added last), or the gather
 // v_c[a] = P_c[a][s] for a leaf in state s (1 for a marginalised leaf: P rows
 // sum to 1 after the row rule).  Then alpha_i = v_l * v_r, and each column is
 // rescaled by an exact power of two so its maximum lies in [0.5,1); the
@@ -371,7 +428,7 @@ struct PruneSmem {
     }
 };
 
-template <typename T, int TC>
+template <typename T, int TC, bool KAHAN>
 __device__ inline void child_partial(const T *Et, const T *slots, int slot, int leaf, const uint8_t *lvT, int a0,
                                      int c0, T v[4][TC / 16])
 {
@@ -389,13 +446,15 @@ __device__ inline void child_partial(const T *Et, const T *slots, int slot, int 
         return;
     }
     const T *al = slots + (size_t)slot * K * TC;
+    // sum_j E[a][j] alpha[j] accumulated separately from alpha[a] (added last)
+    T acc[4][CPT], comp[4][CPT];
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-        T x[CPT];
-        ColLoad<T, CPT>::load(al + (a0 + i) * TC + c0, x);
+    for (int i = 0; i < 4; i++)
 #pragma unroll
-        for (int cc = 0; cc < CPT; cc++) v[i][cc] = x[cc];
-    }
+        for (int cc = 0; cc < CPT; cc++) {
+            acc[i][cc] = (T)0;
+            comp[i][cc] = (T)0;
+        }
 #pragma unroll 4
     for (int j = 0; j < K; j++) {
         T e[4], x[CPT];
@@ -404,11 +463,29 @@ __device__ inline void child_partial(const T *Et, const T *slots, int slot, int 
 #pragma unroll
         for (int i = 0; i < 4; i++)
 #pragma unroll
-            for (int cc = 0; cc < CPT; cc++) v[i][cc] += e[i] * x[cc];
+            for (int cc = 0; cc < CPT; cc++) {
+                if (KAHAN) {
+                    // compensated summation: the rounding error of each addition is
+                    // carried in comp, so small terms are not lost against a large sum
+                    T y = e[i] * x[cc] - comp[i][cc];
+                    T t = acc[i][cc] + y;
+                    comp[i][cc] = (t - acc[i][cc]) - y;
+                    acc[i][cc] = t;
+                } else {
+                    acc[i][cc] += e[i] * x[cc];
+                }
+            }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        T x[CPT];
+        ColLoad<T, CPT>::load(al + (a0 + i) * TC + c0, x);
+#pragma unroll
+        for (int cc = 0; cc < CPT; cc++) v[i][cc] = x[cc] + (acc[i][cc] - comp[i][cc]);
     }
 }
 
-template <typename T, int TC>
+template <typename T, int TC, bool KAHAN>
 __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
 {
     constexpr int CPT = TC / 16;
@@ -460,8 +537,8 @@ __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
             }
             __syncthreads();
             T vl[4][CPT], vr[4][CPT];
-            child_partial<T, TC>(Et, slots, sn.lslot, sn.lc, lvT, a0, c0, vl);
-            child_partial<T, TC>(Et + K2, slots, sn.rslot, sn.rc, lvT, a0, c0, vr);
+            child_partial<T, TC, KAHAN>(Et, slots, sn.lslot, sn.lc, lvT, a0, c0, vl);
+            child_partial<T, TC, KAHAN>(Et + K2, slots, sn.rslot, sn.rc, lvT, a0, c0, vr);
             __syncthreads();
             MU *cm = colmax + (ni & 1) * TC;
             MU *cm_next = colmax + ((ni + 1) & 1) * TC;
@@ -535,21 +612,22 @@ size_t prune_smem_bytes(int prec, int nslots, int nl, int nint)
     return PruneSmem<float, 64>::bytes(nslots, nl, nint);
 }
 
-template <typename T, int TC>
+template <typename T, int TC, bool KAHAN>
 static cudaError_t launch_prune_t(const PruneArgs &a, cudaStream_t s, int grid)
 {
     size_t smem = PruneSmem<T, TC>::bytes(a.nslots, a.nl, a.n_internal);
-    cudaError_t e = cudaFuncSetAttribute(k_prune<T, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_prune<T, TC, KAHAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_prune<T, TC><<<grid, PR_THREADS, smem, s>>>(a);
+    k_prune<T, TC, KAHAN><<<grid, PR_THREADS, smem, s>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_prune(int prec, const PruneArgs &a, cudaStream_t s, int grid)
+cudaError_t launch_prune(int prec, bool compensated, const PruneArgs &a, cudaStream_t s, int grid)
 {
     if (a.nwi <= 0) return cudaSuccess;
-    if (prec == PCSF_PREC_FP64) return launch_prune_t<double, 32>(a, s, grid);
-    return launch_prune_t<float, 64>(a, s, grid);
+    if (prec == PCSF_PREC_FP64) return launch_prune_t<double, 32, false>(a, s, grid);
+    if (compensated) return launch_prune_t<float, 64, true>(a, s, grid);
+    return launch_prune_t<float, 64, false>(a, s, grid);
 }
 
 // ---------------------------------------------------------------------------

@@ -54,6 +54,15 @@ struct DevModels {
     const double *prior;    // [2][K]     root prior
     const double *wlog;     // [2][K]     prior_a * log(prior_a)
     double tol;             // Q.Diag tol (1e-6)
+    // FP32 P(t) formation: E(t) = E(t_g) + D^-1/2 U diag(e^{lam t} - e^{lam t_g}) U^T D^1/2
+    // around the nearest point t_g of a geometric grid whose E(t_g) were formed
+    // in FP64; below the first grid point E(t) = t Q + t^2/2 Q^2.
+    const float *gridT;     // [2][G][K][K]  E(t_g)^T in FP32
+    const double *grid_t;   // [G]
+    int grid_n;
+    double grid_lr;         // log of the grid ratio
+    const float *Qf;        // [2][K][K]  Q (row-major)
+    const float *Q2f;       // [2][K][K]  Q^2
 };
 
 // Status keys: ((branch*K + row) << 4) | code, min-reduced so the first error
@@ -70,8 +79,10 @@ cudaError_t launch_jacobi(const double *A, double *U, double *lam, int *status, 
 
 // P(t) formation for P sets [nps]: writes E^T = (P - I)^T per branch into
 // Pbuf ([nps][nbr][K][K], element (j,i) = E[i][j]) in FP64 or FP32.
+// raw = true skips the row rule (used to form the FP64 grid itself).
 cudaError_t launch_pform(bool fp64, const PSet *ps, int nps, const double *branch, int nbr,
-                         DevModels m, void *Pbuf, int32_t *status_key, cudaStream_t s);
+                         DevModels m, void *Pbuf, int32_t *status_key, cudaStream_t s, bool raw = false);
+cudaError_t launch_d2f(const double *in, float *out, size_t n, cudaStream_t s);
 
 // Pruning over work items [nwi]; partials [nwi][2] (lpr, elpr).
 struct PruneArgs {
@@ -88,7 +99,7 @@ struct PruneArgs {
     DevModels m;
     double *partials;        // [nwi][2]
 };
-cudaError_t launch_prune(int prec, const PruneArgs &a, cudaStream_t s, int grid);
+cudaError_t launch_prune(int prec, bool compensated, const PruneArgs &a, cudaStream_t s, int grid);
 int prune_tile_cols(int prec);
 size_t prune_smem_bytes(int prec, int nslots, int nl, int nint);
 

@@ -26,7 +26,8 @@ STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memo
                 9: "CamlPaml.P14n.instantiate_q: Q scale evaluated to a non-positive value",
                 10: "capacity exceeded"}
 FIXED, MLE = 0, 1
-PREC = {"fp64": 0, "fp32": 1, "tf32x3": 2, "bf16x3": 3, "tf32": 4}
+PREC = {"fp64": 0, "fp32": 1, "tf32x3": 2, "bf16x3": 3, "tf32": 4,
+        "fp32c": 1 | (1 << 16)}     # fp32c: FP32 contractions with compensated summation
 MARGINALIZE = 64
 ORF_MODES = {"asis": 0, "atgstop": 1, "stopstop": 2, "stopstop3": 3, "tofirststop": 4,
              "fromlaststop": 5, "toorfromstop": 6}
