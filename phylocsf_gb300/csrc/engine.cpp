@@ -129,12 +129,21 @@ struct pcsf_engine {
     DevBuf<WorkItem> dwi;
     DevBuf<int32_t> dwib, dstatus;
     DevBuf<double> dpart, dlpr, delpr;
+    // gradient path
+    DevBuf<unsigned char> gscratch;
+    DevBuf<double> dgpart, dgrad;
+    DevBuf<float> dQrowf;
+    DevBuf<double> dQrowd;
+    HostBuf<double> hgrad;
+    int grad_grid = 0;
     HostBuf<PSet> hps;
     HostBuf<Request> hreq;
     HostBuf<WorkItem> hwi;
     HostBuf<int32_t> hwib, hstatus;
     HostBuf<double> hlpr, helpr;
     int prune_grid = 0;
+    int sm_count = 0;
+    DevBuf<int> derr;     // set by a kernel whose bounded wait timed out
 
     pcsf_stats stats{};
 
@@ -412,6 +421,21 @@ static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2],
     e->dm.wlog = e->dwlog.p;
     e->dm.tol = e->tol;
     e->dm.grid_n = 0;
+    {
+        // Q row-major in both arithmetic types, for dP/dt = Q P(t) in the gradient
+        std::vector<double> qd(2 * K2);
+        std::vector<float> qf(2 * K2);
+        for (int m = 0; m < 2; m++)
+            for (int i = 0; i < K2; i++) {
+                qd[m * K2 + i] = Q[m][i];
+                qf[m * K2 + i] = (float)Q[m][i];
+            }
+        CK(e->dQrowd.reserve(2 * K2), "cudaMalloc");
+        CK(e->dQrowf.reserve(2 * K2), "cudaMalloc");
+        CK(cudaMemcpyAsync(e->dQrowd.p, qd.data(), sizeof(double) * 2 * K2, cudaMemcpyHostToDevice, e->stream), "H2D");
+        CK(cudaMemcpyAsync(e->dQrowf.p, qf.data(), sizeof(float) * 2 * K2, cudaMemcpyHostToDevice, e->stream), "H2D");
+        CK(cudaStreamSynchronize(e->stream), "Q upload");
+    }
     if (e->prec != PCSF_PREC_FP64) {
         int rc = build_pt_grid(e, Q);
         if (rc) return rc;
@@ -422,7 +446,7 @@ static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2],
 static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t flags)
 {
     int prec = flags & 0xff;
-    if (prec != PCSF_PREC_FP64 && prec != PCSF_PREC_FP32)
+    if (prec != PCSF_PREC_FP64 && prec != PCSF_PREC_FP32 && prec != PCSF_PREC_TF32X3 && prec != PCSF_PREC_TF32)
         return e->fail(PCSF_EINVAL, "precision mode %d is not available in this build", prec);
     e->prec = prec;
     e->compensated = (flags & PCSF_COMPENSATED) != 0;
@@ -448,6 +472,15 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
     CK(cudaMemcpyAsync(e->dbranch.p, e->branch.data(), sizeof(double) * e->nbr, cudaMemcpyHostToDevice, e->stream), "H2D");
     CK(cudaMemcpyAsync(e->dsched.p, e->sched.data(), sizeof(SchedNode) * e->sched.size(), cudaMemcpyHostToDevice,
                        e->stream), "H2D");
+    e->sm_count = prop.multiProcessorCount;
+    CK(e->derr.reserve(1), "cudaMalloc");
+    CK(cudaMemsetAsync(e->derr.p, 0, sizeof(int), e->stream), "memset");
+    const bool tc = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
+    if (tc && !prune_tc_supported(e->nslots, e->nl))
+        return e->fail(PCSF_EINVAL, "tensor-core path supports up to 160 leaves and 6 partial slots (tree: %d, %d)",
+                       e->nl, e->nslots);
+    if (tc && prune_tc_smem_bytes(e->nl) > (size_t)prop.sharedMemPerBlockOptin)
+        return e->fail(PCSF_EINVAL, "tensor-core path needs %zu B shared memory", prune_tc_smem_bytes(e->nl));
     size_t smem = prune_smem_bytes(e->prec, e->nslots, e->nl, (int)e->sched.size());
     if (smem > (size_t)prop.sharedMemPerBlockOptin)
         return e->fail(PCSF_EINVAL, "tree needs %d partial slots (%zu B shared memory > %zu)", e->nslots, smem,
@@ -455,6 +488,11 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
     int per_sm = std::max(1, (int)(prop.sharedMemPerMultiprocessor / (smem + 1024)));
     per_sm = std::min(per_sm, 8);
     e->prune_grid = prop.multiProcessorCount * per_sm;
+    size_t gsmem = grad_smem_bytes(e->prec, e->nslots, e->nl, (int)e->sched.size());
+    if (gsmem > (size_t)prop.sharedMemPerBlockOptin)
+        return e->fail(PCSF_EINVAL, "tree needs %zu B shared memory for the gradient", gsmem);
+    int gper = std::max(1, std::min(4, (int)(prop.sharedMemPerMultiprocessor / (gsmem + 1024))));
+    e->grad_grid = prop.multiProcessorCount * gper;
     // P(t) buffer: up to 4 GiB, at most a quarter of free memory
     size_t freeb = 0, totalb = 0;
     CK(cudaMemGetInfo(&freeb, &totalb), "cudaMemGetInfo");
@@ -472,12 +510,16 @@ struct Eval {
     int status;
 };
 
-static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &reqs_in, std::vector<Eval> &out)
+// grad (optional): d lpr / d t_c per request, [nreq][nbr], by the adjoint kernel.
+static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &reqs_in, std::vector<Eval> &out,
+                    std::vector<double> *grad = nullptr)
 {
     const int nreq = (int)reqs_in.size();
     out.assign(nreq, Eval{0.0, 0.0, PCSF_OK});
     if (nreq == 0) return PCSF_OK;
-    const int TC = prune_tile_cols(e->prec);
+    const bool tc = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
+    // the gradient always runs the SIMT adjoint kernel (64-column tiles in FP32)
+    const int TC = grad ? (e->prec == PCSF_PREC_FP64 ? 32 : 64) : prune_tile_cols(e->prec);
 
     // work items, P-set dedup and chunking (at most pbuf_psets distinct P sets per chunk)
     std::vector<Request> reqs(reqs_in);
@@ -546,6 +588,14 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     for (size_t c = 0; c + 1 < chunk_ps_begin.size(); c++)
         max_chunk_ps = std::max<size_t>(max_chunk_ps, chunk_ps_begin[c + 1] - chunk_ps_begin[c]);
     CK(e->Pbuf.reserve(max_chunk_ps * pset_bytes), "cudaMalloc P(t) buffer");
+    size_t gscr = 0;
+    if (grad) {
+        gscr = grad_scratch_per_cta(e->prec, e->nl);
+        CK(e->gscratch.reserve(gscr * (size_t)e->grad_grid), "cudaMalloc gradient scratch");
+        CK(e->dgpart.reserve((size_t)std::max(nwi, 1) * e->nbr), "cudaMalloc");
+        CK(e->dgrad.reserve((size_t)nreq * e->nbr), "cudaMalloc");
+        CK(e->hgrad.reserve((size_t)nreq * e->nbr), "cudaMallocHost");
+    }
 
     std::memcpy(e->hps.p, psets.data(), sizeof(PSet) * nps);
     std::memcpy(e->hreq.p, reqs.data(), sizeof(Request) * nreq);
@@ -580,8 +630,34 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         pa.nslots = e->nslots;
         pa.m = e->dm;
         pa.partials = e->dpart.p + 2 * (size_t)wib[r0];
-        int grid = std::min(e->prune_grid, std::max(pa.nwi, 1));
-        CK(launch_prune(e->prec, e->compensated, pa, s, grid), "pruning launch");
+        if (grad) {
+            GradArgs ga{};
+            ga.wi = pa.wi;
+            ga.nwi = pa.nwi;
+            ga.req = pa.req;
+            ga.leaves = pa.leaves;
+            ga.Pbuf = pa.Pbuf;
+            ga.sched = pa.sched;
+            ga.n_internal = pa.n_internal;
+            ga.nl = pa.nl;
+            ga.nbr = pa.nbr;
+            ga.nslots = pa.nslots;
+            ga.m = pa.m;
+            ga.Qrow = e->prec == PCSF_PREC_FP64 ? (const void *)e->dQrowd.p : (const void *)e->dQrowf.p;
+            ga.scratch = e->gscratch.p;
+            ga.scratch_per_cta = gscr;
+            ga.partials = pa.partials;
+            ga.gpart = e->dgpart.p + (size_t)wib[r0] * e->nbr;
+            int grid = std::min(e->grad_grid, std::max(pa.nwi, 1));
+            CK(launch_grad(e->prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32,
+                           e->compensated || tc, ga, s, grid), "gradient launch");
+        } else if (tc) {
+            int grid = std::min(e->sm_count, std::max(pa.nwi, 1));
+            CK(launch_prune_tc(e->prec == PCSF_PREC_TF32X3 ? 3 : 1, pa, e->derr.p, s, grid), "tensor-core pruning launch");
+        } else {
+            int grid = std::min(e->prune_grid, std::max(pa.nwi, 1));
+            CK(launch_prune(e->prec, e->compensated, pa, s, grid), "pruning launch");
+        }
         CK(cudaEventRecord(e->ev[2], s), "event");
         e->stats.pform_launches += (p1 > p0);
         e->stats.prune_launches += (pa.nwi > 0);
@@ -595,12 +671,20 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     }
     CK(cudaEventRecord(e->ev[3], s), "event");
     CK(launch_reduce(e->dpart.p, e->dwib.p, nreq, e->dlpr.p, e->delpr.p, s), "reduce launch");
-    CK(cudaEventRecord(e->ev[4], s), "event");
     e->stats.kernel_launches += 1;
+    if (grad) {
+        CK(launch_reduce_grad(e->dgpart.p, e->dwib.p, nreq, e->nbr, e->dgrad.p, s), "gradient reduce launch");
+        e->stats.kernel_launches += 1;
+        CK(cudaMemcpyAsync(e->hgrad.p, e->dgrad.p, sizeof(double) * nreq * e->nbr, cudaMemcpyDeviceToHost, s), "D2H grad");
+    }
+    CK(cudaEventRecord(e->ev[4], s), "event");
     CK(cudaMemcpyAsync(e->hlpr.p, e->dlpr.p, sizeof(double) * nreq, cudaMemcpyDeviceToHost, s), "D2H lpr");
     CK(cudaMemcpyAsync(e->helpr.p, e->delpr.p, sizeof(double) * nreq, cudaMemcpyDeviceToHost, s), "D2H elpr");
     CK(cudaMemcpyAsync(e->hstatus.p, e->dstatus.p, sizeof(int32_t) * nps, cudaMemcpyDeviceToHost, s), "D2H status");
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, e->derr.p, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H error flag");
     CK(cudaStreamSynchronize(s), "evaluation");
+    if (herr) return e->fail(PCSF_ECUDA, "a tensor-core wait timed out; results of this call are invalid");
     float rd_ms = 0.f;
     cudaEventElapsedTime(&rd_ms, e->ev[3], e->ev[4]);
     e->stats.pform_ms += pf_ms;
@@ -611,15 +695,26 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         int st = (key >= 0 && key < 0x7f000000) ? (key & 15) : PCSF_OK;
         out[r] = Eval{e->hlpr.p[r], e->helpr.p[r], st};
     }
+    if (grad) grad->assign(e->hgrad.p, e->hgrad.p + (size_t)nreq * e->nbr);
     return PCSF_OK;
 }
 
 // ---------------------------------------------------------------------------
 // One maximize_lpr (PhyloCSFModel.ml:84-99) as a resumable state machine.
 
+// In reduced precision the objective carries rounding noise of ~1e-7 relative,
+// larger than the change of lpr over Brent's smallest probes (sqrt(eps)|x|).
+// A trial point within DERIV_REL*|x| of the best point is therefore valued
+// by the first-order expansion f(x) + f'(x)(u - x) with f'(x) from the
+// adjoint pass (second-order remainder < 1e-8 relative); every reported value
+// is still a direct evaluation.
+constexpr double DERIV_REL = 1e-4;
+
 struct Fit {
     int region = 0, model = 0;
     int64_t ncols = 0;
+    bool deriv = false;   // derivative-assisted small steps (reduced precision)
+    std::deque<std::pair<double, double>> gcache;   // rho -> d lpr / d rho
     double lo = 1e-2, hi = 10.0, init = 1.0, accuracy = 0.01;
     int maxtries = 250;
     enum Phase { FI_START, FI_LOOP, BR_SET, BR_V, BR_PROPOSE, BR_ACCEPT, FINAL, DONE } phase = FI_START;
@@ -642,10 +737,17 @@ struct Fit {
             if (c.first == r) return &c.second;
         return nullptr;
     }
+    const double *getg(double r) const
+    {
+        for (auto &c : gcache)
+            if (c.first == r) return &c.second;
+        return nullptr;
+    }
 };
 
-// Advance until a value outside the cache is needed (appended to `need`) or done.
-static void advance(Fit &f, std::vector<double> &need)
+// Advance until a value outside the cache is needed (appended to `need`, or to
+// `need_grad` for a gradient) or done.
+static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need_grad)
 {
     auto ask = [&](double r) -> const Eval * {
         const Eval *ev = f.get(r);
@@ -773,10 +875,23 @@ static void advance(Fit &f, std::vector<double> &need)
             break;
         }
         case Fit::BR_ACCEPT: {
-            const Eval *a = ask(f.u);
-            if (!a) return;
-            if (failed(a)) return;
-            const double u = f.u, fu = -a->lpr;
+            double fu;
+            const double u = f.u;
+            if (f.deriv && std::fabs(u - f.bx) <= DERIV_REL * std::fabs(f.bx) && f.ncols > 0) {
+                const Eval *bx = f.get(f.bx);
+                const double *g = f.getg(f.bx);
+                if (!bx || !g) {
+                    need_grad.push_back(f.bx);
+                    return;
+                }
+                if (failed(bx)) return;
+                fu = -(bx->lpr + (*g) * (u - f.bx));
+            } else {
+                const Eval *a = ask(u);
+                if (!a) return;
+                if (failed(a)) return;
+                fu = -a->lpr;
+            }
             if (fu <= f.bfx) {
                 if (u < f.bx) { f.bhi = f.bx; f.bfhi = f.bfx; }
                 else { f.blo = f.bx; f.bflo = f.bfx; }
@@ -824,23 +939,31 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
     // PCSF_TRACE_REGION=<r>: print every evaluation of region r's fits to stderr
     const char *tr = std::getenv("PCSF_TRACE_REGION");
     const int trace = tr ? std::atoi(tr) : -1;
-    std::vector<Request> reqs;
-    std::vector<std::pair<int, double>> owner;
-    std::vector<Eval> res;
+    std::vector<Request> reqs, greqs;
+    std::vector<std::pair<int, double>> owner, gowner;
+    std::vector<Eval> res, gres;
+    std::vector<double> grad;
     for (;;) {
         reqs.clear();
         owner.clear();
+        greqs.clear();
+        gowner.clear();
         for (int i = 0; i < (int)fits.size(); i++) {
-            std::vector<double> need;
-            advance(fits[i], need);
-            std::sort(need.begin(), need.end());
-            need.erase(std::unique(need.begin(), need.end()), need.end());
+            std::vector<double> need, needg;
+            advance(fits[i], need, needg);
+            for (auto *lst : {&need, &needg}) {
+                std::sort(lst->begin(), lst->end());
+                lst->erase(std::unique(lst->begin(), lst->end()), lst->end());
+            }
+            bool bad = false;
+            for (double r : need) bad |= !(r > 0.0) || !std::isfinite(r);
+            for (double r : needg) bad |= !(r > 0.0) || !std::isfinite(r);
+            if (bad) {
+                fits[i].status = PCSF_EINVAL;
+                fits[i].phase = Fit::DONE;
+                continue;
+            }
             for (double r : need) {
-                if (!(r > 0.0) || !std::isfinite(r)) {
-                    fits[i].status = PCSF_EINVAL;
-                    fits[i].phase = Fit::DONE;
-                    break;
-                }
                 Request q{};
                 q.region = fits[i].region;
                 q.model = fits[i].model;
@@ -848,11 +971,25 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
                 reqs.push_back(q);
                 owner.push_back({i, r});
             }
+            for (double r : needg) {
+                Request q{};
+                q.region = fits[i].region;
+                q.model = fits[i].model;
+                q.rho = r;
+                greqs.push_back(q);
+                gowner.push_back({i, r});
+            }
         }
-        if (reqs.empty()) break;
+        if (reqs.empty() && greqs.empty()) break;
         e->stats.rounds += 1;
-        int rc = evaluate(e, b, reqs, res);
-        if (rc) return rc;
+        if (!reqs.empty()) {
+            int rc = evaluate(e, b, reqs, res);
+            if (rc) return rc;
+        }
+        if (!greqs.empty()) {
+            int rc = evaluate(e, b, greqs, gres, &grad);
+            if (rc) return rc;
+        }
         for (size_t k = 0; k < reqs.size(); k++) {
             Fit &f = fits[owner[k].first];
             f.cache.push_back({owner[k].second, res[k]});
@@ -860,6 +997,17 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
                 std::fprintf(stderr, "trace region %d model %d round %lld rho %.17g lpr %.17g status %d | phase %d bx %.17g [%.17g %.17g]\n",
                              f.region, f.model, (long long)e->stats.rounds, owner[k].second, res[k].lpr, res[k].status,
                              (int)f.phase, f.bx, f.blo, f.bhi);
+        }
+        for (size_t k = 0; k < greqs.size(); k++) {
+            Fit &f = fits[gowner[k].first];
+            const double r = gowner[k].second;
+            double dr = 0.0;
+            for (int c = 0; c < e->nbr; c++) dr += e->branch[c] * grad[k * e->nbr + c];
+            f.gcache.push_back({r, dr});
+            if (!f.get(r)) f.cache.push_back({r, gres[k]});
+            if (f.region == trace)
+                std::fprintf(stderr, "trace region %d model %d round %lld grad at rho %.17g lpr %.17g dlpr/drho %.17g\n",
+                             f.region, f.model, (long long)e->stats.rounds, r, gres[k].lpr, dr);
         }
     }
     return PCSF_OK;
@@ -876,6 +1024,7 @@ static int score_impl(pcsf_engine *e, pcsf_batch *b, int strategy, pcsf_result *
             f.region = r;
             f.model = m;
             f.ncols = b->offs[r + 1] - b->offs[r];
+            f.deriv = e->prec != PCSF_PREC_FP64;
             if (strategy == PCSF_FIXED) {
                 // llr_FixedLik 1.0: a single evaluation at rho = 1
                 f.x = 1.0;
@@ -897,7 +1046,7 @@ static int score_impl(pcsf_engine *e, pcsf_batch *b, int strategy, pcsf_result *
         o.elpr_n = nf.elpr;
         o.score = decibans(c.lpr - nf.lpr);
         o.anc_comp_score = decibans(c.elpr - nf.elpr);
-        o.evals = (int32_t)(c.cache.size() + nf.cache.size());
+        o.evals = (int32_t)(c.cache.size() + nf.cache.size() + c.gcache.size() + nf.gcache.size());
     }
     return PCSF_OK;
 }
@@ -1148,9 +1297,33 @@ int pcsf_lpr(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, do
 int pcsf_grad(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, double *lpr, double *d_branch,
               double *d_rho, int32_t *status)
 {
-    (void)b; (void)model; (void)rho; (void)lpr; (void)d_branch; (void)d_rho; (void)status;
     if (!e) return PCSF_EINVAL;
-    return e->fail(PCSF_EINVAL, "pcsf_grad: the adjoint kernel is not built yet");
+    CK(cudaSetDevice(e->device), "cudaSetDevice");
+    if (!b || b->e != e) return e->fail(PCSF_EINVAL, "pcsf_grad: batch does not belong to this engine");
+    if (model < 0 || model > 1) return e->fail(PCSF_EINVAL, "pcsf_grad: model %d", model);
+    if (b->nreg > 0 && (!rho || !lpr)) return e->fail(PCSF_EINVAL, "pcsf_grad: null output");
+    std::vector<Request> reqs(b->nreg);
+    for (int r = 0; r < b->nreg; r++) {
+        if (!(rho[r] > 0.0) || !std::isfinite(rho[r])) return e->fail(PCSF_EINVAL, "pcsf_grad: rho[%d] = %g", r, rho[r]);
+        reqs[r] = Request{r, model, 0, 0, rho[r]};
+    }
+    std::vector<Eval> res;
+    std::vector<double> g;
+    int rc = evaluate(e, b, reqs, res, &g);
+    if (rc) return rc;
+    for (int r = 0; r < b->nreg; r++) {
+        lpr[r] = res[r].lpr;
+        if (status) status[r] = res[r].status;
+        // t_c = rho * b_c: d lpr / d rho = sum_c b_c d lpr / d t_c
+        double dr = 0.0;
+        for (int c = 0; c < e->nbr; c++) {
+            double gc = g[(size_t)r * e->nbr + c];
+            if (d_branch) d_branch[(size_t)r * e->nbr + c] = gc;
+            dr += e->branch[c] * gc;
+        }
+        if (d_rho) d_rho[r] = dr;
+    }
+    return PCSF_OK;
 }
 
 }  // extern "C"

@@ -1,0 +1,332 @@
+// Adjoint (outside-pass) gradient of the log-likelihood with respect to every
+// branch length, for a batch of (region, model, rho) requests.
+//
+// Reference mathematics (paths relative to mlin/PhyloCSF):
+//   outside pass          lib/CamlPaml/PhyloLik.ml:96-120   beta_i = P_i^T (beta_p . (P_s alpha_s))
+//   branch posteriors     lib/CamlPaml/PhyloLik.ml:140-174
+//   dP/dt                 lib/CamlPaml/Q.ml:260-275          dP/dt = Q P(t)
+//   d ELL / d branch      lib/CamlPaml/PhyloEM.ml:140-171    (Fisher identity: = d logL / d t)
+// Per column, with v_c = P_c alpha_c the partial of child c at its parent p and
+// s its sibling:
+//   inter_c = beta_p . v_s,   d log z / d t_c = inter_c^T Q v_c / z,   beta_c = P_c^T inter_c.
+//
+// One CTA (256 threads) owns a tile of TC columns.  The inside pass is the one of
+// k_prune but also stores every child partial v_c and the per-column exponents
+// of the power-of-two rescaling in a per-CTA global scratch area; the outside
+// pass then walks the schedule in reverse.  Exponent bookkeeping per column:
+// alpha_i = alpha~_i 2^{e(i)} with e(i) = e(l) + e(r) + s_i, beta_c = beta~_c 2^{f(c)}
+// with f(c) = f(p) + e(s) + t_c, and the gradient term carries
+// 2^{f(p) + e(s) + e(c) - e(root)} against the scaled z~.
+#include <cmath>
+
+#include "pcsf_internal.h"
+#include "prune_common.cuh"
+
+namespace pcsf {
+
+constexpr int GR_THREADS = 256;
+
+template <typename T, int TC>
+struct GradLayout {
+    static size_t smem(int nslots, int nl, int nint)
+    {
+        size_t b = sizeof(T) * (3 * (size_t)K2 + (size_t)nslots * K * TC + (size_t)K * TC + 16 * TC);
+        b += sizeof(typename AtomMax<T>::U) * TC;
+        b += sizeof(double) * TC + sizeof(int) * 2 * TC;
+        b += sizeof(SchedNode) * nint;
+        b = (b + 15) & ~size_t(15);
+        b += (size_t)nl * TC;
+        return (b + 15) & ~size_t(15);
+    }
+    static size_t scratch(int nl)
+    {
+        const int n = 2 * nl - 1;
+        size_t b = sizeof(T) * ((size_t)(n - 1) + (nl - 1)) * K * TC;
+        b += sizeof(int) * 2 * (size_t)n * TC;
+        return (b + 255) & ~size_t(255);
+    }
+};
+
+template <typename T, int TC, bool KAHAN>
+__global__ void __launch_bounds__(GR_THREADS) k_grad(GradArgs a)
+{
+    constexpr int CPT = TC / 16;
+    typedef typename AtomMax<T>::U MU;
+    extern __shared__ __align__(16) unsigned char gsm[];
+    T *Mat = reinterpret_cast<T *>(gsm);                          // [3][K][K]
+    T *slots = Mat + 3 * K2;                                       // [nslots][K][TC]
+    T *X = slots + (size_t)a.nslots * K * TC;                      // [K][TC]
+    T *red = X + K * TC;                                           // [16][TC]
+    MU *colmax = reinterpret_cast<MU *>(red + 16 * TC);            // [TC]
+    double *zt = reinterpret_cast<double *>(colmax + TC);          // [TC]
+    int *eroot = reinterpret_cast<int *>(zt + TC);                 // [TC]
+    int *sexp = eroot + TC;                                        // [TC]
+    SchedNode *sched = reinterpret_cast<SchedNode *>(sexp + TC);   // [n_internal]
+    size_t off = (reinterpret_cast<unsigned char *>(sched + a.n_internal) - gsm + 15) & ~size_t(15);
+    uint8_t *lvT = gsm + off;                                      // [nl][TC]
+    __shared__ double wsum_l[GR_THREADS / 32], wsum_e[GR_THREADS / 32];
+
+    const int tid = threadIdx.x;
+    const int ty = tid / 16, tx = tid % 16;
+    const int a0 = 4 * ty, c0 = CPT * tx;
+    const int nl = a.nl, n = 2 * nl - 1;
+    unsigned char *sbase = reinterpret_cast<unsigned char *>(a.scratch) + (size_t)blockIdx.x * a.scratch_per_cta;
+    T *V = reinterpret_cast<T *>(sbase);                             // [n-1][K][TC]
+    T *B = V + (size_t)(n - 1) * K * TC;                             // [nl-1][K][TC] (internal nodes)
+    int *eS = reinterpret_cast<int *>(B + (size_t)(nl - 1) * K * TC);  // [n][TC]
+    int *fS = eS + (size_t)n * TC;                                   // [n][TC]
+    auto e_of = [&](int node, int col) -> int { return node < nl ? 0 : eS[(size_t)node * TC + col]; };
+
+    for (int f = tid; f < a.n_internal; f += GR_THREADS) sched[f] = a.sched[f];
+
+    for (int w = blockIdx.x; w < a.nwi; w += gridDim.x) {
+        const WorkItem wi = a.wi[w];
+        const Request rq = a.req[wi.request];
+        const int md = rq.model;
+        const T *Pbase = reinterpret_cast<const T *>(a.Pbuf) + (size_t)rq.pset * a.nbr * K2;
+        const int ncols = wi.ncols;
+        const uint8_t *lg = a.leaves + (size_t)wi.col0 * nl;
+        __syncthreads();
+        for (int f = tid; f < TC * nl; f += GR_THREADS) {
+            int c = f / nl, l = f - c * nl;
+            lvT[l * TC + c] = (c < ncols) ? lg[f] : (uint8_t)K;
+        }
+        for (int f = tid; f < TC; f += GR_THREADS) colmax[f] = 0;
+        {
+            const T *Qg = reinterpret_cast<const T *>(a.Qrow) + (size_t)md * K2;
+            for (int f = tid; f < K2; f += GR_THREADS) Mat[2 * K2 + f] = Qg[f];
+        }
+
+        // ---------------- inside pass, storing the child partials
+        for (int ni = 0; ni < a.n_internal; ni++) {
+            const SchedNode sn = sched[ni];
+            {
+                const float4 *gl = reinterpret_cast<const float4 *>(Pbase + (size_t)sn.lc * K2);
+                const float4 *gr = reinterpret_cast<const float4 *>(Pbase + (size_t)sn.rc * K2);
+                float4 *sl = reinterpret_cast<float4 *>(Mat);
+                float4 *sr = reinterpret_cast<float4 *>(Mat + K2);
+                constexpr int NV = K2 * sizeof(T) / 16;
+                for (int f = tid; f < NV; f += GR_THREADS) {
+                    sl[f] = __ldg(gl + f);
+                    sr[f] = __ldg(gr + f);
+                }
+            }
+            __syncthreads();
+            T vl[4][CPT], vr[4][CPT];
+            child_partial<T, TC, KAHAN>(Mat, slots, sn.lslot, sn.lc, lvT, a0, c0, vl);
+            child_partial<T, TC, KAHAN>(Mat + K2, slots, sn.rslot, sn.rc, lvT, a0, c0, vr);
+            T mxc[CPT];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int cc = 0; cc < CPT; cc++) {
+                    V[((size_t)sn.lc * K + a0 + i) * TC + c0 + cc] = vl[i][cc];
+                    V[((size_t)sn.rc * K + a0 + i) * TC + c0 + cc] = vr[i][cc];
+                }
+            __syncthreads();   // Mat and slots reads done; colmax zeroed
+#pragma unroll
+            for (int cc = 0; cc < CPT; cc++) {
+                T mx = (T)0;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    vl[i][cc] *= vr[i][cc];
+                    mx = vl[i][cc] > mx ? vl[i][cc] : mx;
+                }
+                mxc[cc] = mx;
+                AtomMax<T>::upd(colmax + c0 + cc, mx);
+            }
+            __syncthreads();
+            T *out = slots + (size_t)sn.oslot * K * TC;
+#pragma unroll
+            for (int cc = 0; cc < CPT; cc++) {
+                T mx = AtomMax<T>::get(colmax + c0 + cc);
+                int e = (mx > (T)0) ? exp_of(mx) : 0;
+#pragma unroll
+                for (int i = 0; i < 4; i++) out[(a0 + i) * TC + c0 + cc] = scale2(vl[i][cc], -e);
+                if (ty == 0) {
+                    const int col = c0 + cc;
+                    eS[(size_t)sn.node * TC + col] = e_of(sn.lc, col) + e_of(sn.rc, col) + e;
+                }
+            }
+            (void)mxc;
+            __syncthreads();   // colmax reads done
+            for (int f = tid; f < TC; f += GR_THREADS) colmax[f] = 0;
+        }
+        __syncthreads();
+        // ---------------- root: z~, lpr and elpr terms
+        const int root = n - 1;
+        double tl = 0.0, te = 0.0;
+        if (tid < TC) {
+            const T *ar = slots + (size_t)sched[a.n_internal - 1].oslot * K * TC;
+            const double *pr = a.m.prior + md * K;
+            const double *wl = a.m.wlog + md * K;
+            double z = 0.0, wz = 0.0;
+            for (int s = 0; s < K; s++) {
+                double x = (double)ar[s * TC + tid];
+                z += x * pr[s];
+                wz += x * wl[s];
+            }
+            zt[tid] = z;
+            eroot[tid] = eS[(size_t)root * TC + tid];
+            if (tid < ncols) {
+                if (z > 0.0) {
+                    tl = log(z) + (double)eroot[tid] * 0.69314718055994530942;
+                    te = wz / z;
+                } else {
+                    tl = -INFINITY;
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            tl += __shfl_down_sync(0xffffffffu, tl, o);
+            te += __shfl_down_sync(0xffffffffu, te, o);
+        }
+        if ((tid & 31) == 0) { wsum_l[tid >> 5] = tl; wsum_e[tid >> 5] = te; }
+        // beta~_root = prior, f(root) = 0
+        {
+            T *Br = B + (size_t)(root - nl) * K * TC;
+            const double *pr = a.m.prior + md * K;
+            for (int f = tid; f < K * TC; f += GR_THREADS) Br[f] = (T)pr[f / TC];
+            for (int f = tid; f < TC; f += GR_THREADS) fS[(size_t)root * TC + f] = 0;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double sl = 0.0, se = 0.0;
+            for (int k = 0; k < (TC + 31) / 32; k++) { sl += wsum_l[k]; se += wsum_e[k]; }
+            a.partials[2 * (size_t)w] = sl;
+            a.partials[2 * (size_t)w + 1] = se;
+        }
+
+        // ---------------- outside pass, parents before children
+        for (int ni = a.n_internal - 1; ni >= 0; ni--) {
+            const SchedNode sn = sched[ni];
+            const int p = sn.node;
+            const T *Bp = B + (size_t)(p - nl) * K * TC;
+            for (int side = 0; side < 2; side++) {
+                const int c = side ? sn.rc : sn.lc;
+                const int s = side ? sn.lc : sn.rc;
+                const bool internal = c >= nl;
+                __syncthreads();   // previous side finished with X, Mat[0], red, colmax, wsum
+                if (internal) {
+                    // E_c in row-major order (the buffer holds E_c^T)
+                    const T *g = Pbase + (size_t)c * K2;
+                    for (int f = tid; f < K2; f += GR_THREADS) {
+                        int b = f / K, aa = f % K;
+                        Mat[aa * K + b] = g[f];
+                    }
+                }
+                for (int f = tid; f < TC; f += GR_THREADS) colmax[f] = 0;
+                const T *Vs = V + (size_t)s * K * TC;
+                for (int f = tid; f < K * TC; f += GR_THREADS) X[f] = Bp[f] * Vs[f];
+                __syncthreads();
+                // gradient: (Q^T inter) . v_c per column, summed over this thread's 4 states
+                T wq[4][CPT];
+                contract<T, TC, KAHAN>(Mat + 2 * K2, X, a0, c0, wq);
+                const T *Vc = V + (size_t)c * K * TC;
+#pragma unroll
+                for (int cc = 0; cc < CPT; cc++) {
+                    T acc = (T)0;
+#pragma unroll
+                    for (int i = 0; i < 4; i++) acc += wq[i][cc] * Vc[(size_t)(a0 + i) * TC + c0 + cc];
+                    red[ty * TC + c0 + cc] = acc;
+                }
+                T bt[4][CPT];
+                if (internal) {
+                    contract<T, TC, KAHAN>(Mat, X, a0, c0, bt);
+#pragma unroll
+                    for (int cc = 0; cc < CPT; cc++) {
+                        T mx = (T)0;
+#pragma unroll
+                        for (int i = 0; i < 4; i++) {
+                            bt[i][cc] += X[(a0 + i) * TC + c0 + cc];
+                            mx = bt[i][cc] > mx ? bt[i][cc] : mx;
+                        }
+                        AtomMax<T>::upd(colmax + c0 + cc, mx);
+                    }
+                }
+                __syncthreads();
+                if (internal) {
+                    T *Bc = B + (size_t)(c - nl) * K * TC;
+#pragma unroll
+                    for (int cc = 0; cc < CPT; cc++) {
+                        const int col = c0 + cc;
+                        T mx = AtomMax<T>::get(colmax + col);
+                        int e = (mx > (T)0) ? exp_of(mx) : 0;
+#pragma unroll
+                        for (int i = 0; i < 4; i++) Bc[(size_t)(a0 + i) * TC + col] = scale2(bt[i][cc], -e);
+                        if (ty == 0) fS[(size_t)c * TC + col] = fS[(size_t)p * TC + col] + e_of(s, col) + e;
+                    }
+                }
+                double gl = 0.0;
+                if (tid < TC && tid < ncols && zt[tid] > 0.0) {
+                    double sum = 0.0;
+                    for (int k = 0; k < 16; k++) sum += (double)red[k * TC + tid];
+                    const int ex = fS[(size_t)p * TC + tid] + e_of(s, tid) + e_of(c, tid) - eroot[tid];
+                    gl = ldexp(sum, ex) / zt[tid];
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) gl += __shfl_down_sync(0xffffffffu, gl, o);
+                if ((tid & 31) == 0) wsum_l[tid >> 5] = gl;
+                __syncthreads();
+                if (tid == 0) {
+                    double g = 0.0;
+                    for (int k = 0; k < (TC + 31) / 32; k++) g += wsum_l[k];
+                    a.gpart[(size_t)w * a.nbr + c] = g;
+                }
+            }
+        }
+    }
+}
+
+size_t grad_scratch_per_cta(int prec, int nl)
+{
+    if (prec == PCSF_PREC_FP64) return GradLayout<double, 32>::scratch(nl);
+    return GradLayout<float, 64>::scratch(nl);
+}
+
+size_t grad_smem_bytes(int prec, int nslots, int nl, int nint)
+{
+    if (prec == PCSF_PREC_FP64) return GradLayout<double, 32>::smem(nslots, nl, nint);
+    return GradLayout<float, 64>::smem(nslots, nl, nint);
+}
+
+template <typename T, int TC, bool KAHAN>
+static cudaError_t launch_grad_t(const GradArgs &a, cudaStream_t s, int grid)
+{
+    size_t smem = GradLayout<T, TC>::smem(a.nslots, a.nl, a.n_internal);
+    cudaError_t e = cudaFuncSetAttribute(k_grad<T, TC, KAHAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_grad<T, TC, KAHAN><<<grid, GR_THREADS, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grad(int prec, bool compensated, const GradArgs &a, cudaStream_t s, int grid)
+{
+    if (a.nwi <= 0) return cudaSuccess;
+    if (prec == PCSF_PREC_FP64) return launch_grad_t<double, 32, false>(a, s, grid);
+    if (compensated) return launch_grad_t<float, 64, true>(a, s, grid);
+    return launch_grad_t<float, 64, false>(a, s, grid);
+}
+
+// grad[r][c] = sum of gpart over request r's work items (fixed order)
+__global__ void k_reduce_grad(const double *gpart, const int32_t *wi_begin, int nreq, int nbr, double *grad)
+{
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nreq * nbr) return;
+    int r = idx / nbr, c = idx % nbr;
+    double g = 0.0;
+    for (int w = wi_begin[r]; w < wi_begin[r + 1]; w++) g += gpart[(size_t)w * nbr + c];
+    grad[idx] = g;
+}
+
+cudaError_t launch_reduce_grad(const double *gpart, const int32_t *wi_begin, int nreq, int nbr, double *grad,
+                               cudaStream_t s)
+{
+    if (nreq <= 0) return cudaSuccess;
+    int tot = nreq * nbr;
+    k_reduce_grad<<<(tot + 255) / 256, 256, 0, s>>>(gpart, wi_begin, nreq, nbr, grad);
+    return cudaGetLastError();
+}
+
+}  // namespace pcsf

@@ -12,6 +12,7 @@
 #include <cstdio>
 
 #include "pcsf_internal.h"
+#include "prune_common.cuh"
 
 namespace pcsf {
 
@@ -156,23 +157,6 @@ cudaError_t launch_jacobi(const double *A, double *U, double *lam, int *status, 
 
 constexpr int PF_THREADS = 256;
 constexpr int PF_BRANCHES = 4;   // branches per CTA (the eigenvectors are staged once)
-
-template <typename T> struct Vec4;
-template <> struct Vec4<float> {
-    static __device__ inline void load(const float *p, float v[4])
-    {
-        float4 x = *reinterpret_cast<const float4 *>(p);
-        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
-    }
-};
-template <> struct Vec4<double> {
-    static __device__ inline void load(const double *p, double v[4])
-    {
-        double2 x = *reinterpret_cast<const double2 *>(p);
-        double2 y = *reinterpret_cast<const double2 *>(p + 2);
-        v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
-    }
-};
 
 __device__ inline void status_min(int32_t *key, int branch, int row, int code)
 {
@@ -372,45 +356,6 @@ cudaError_t launch_d2f(const double *in, float *out, size_t n, cudaStream_t s)
 // rescaled by an exact power of two so its maximum lies in [0.5,1); the
 // exponents are summed per column and added back as e*ln2 in FP64 at the root.
 
-template <typename T> struct AtomMax;
-template <> struct AtomMax<float> {
-    typedef int U;
-    static __device__ inline void upd(U *p, float v) { atomicMax(p, __float_as_int(v)); }
-    static __device__ inline float get(const U *p) { return __int_as_float(*p); }
-};
-template <> struct AtomMax<double> {
-    typedef unsigned long long U;
-    static __device__ inline void upd(U *p, double v) { atomicMax(p, (unsigned long long)__double_as_longlong(v)); }
-    static __device__ inline double get(const U *p) { return __longlong_as_double((long long)*p); }
-};
-
-template <typename T, int CPT> struct ColLoad;
-template <> struct ColLoad<float, 4> {
-    static __device__ inline void load(const float *p, float v[4]) { Vec4<float>::load(p, v); }
-};
-template <> struct ColLoad<float, 2> {
-    static __device__ inline void load(const float *p, float v[2])
-    {
-        float2 x = *reinterpret_cast<const float2 *>(p);
-        v[0] = x.x; v[1] = x.y;
-    }
-};
-template <> struct ColLoad<double, 2> {
-    static __device__ inline void load(const double *p, double v[2])
-    {
-        double2 x = *reinterpret_cast<const double2 *>(p);
-        v[0] = x.x; v[1] = x.y;
-    }
-};
-template <> struct ColLoad<double, 4> {
-    static __device__ inline void load(const double *p, double v[4]) { Vec4<double>::load(p, v); }
-};
-
-__device__ inline int exp_of(float x) { int e; frexpf(x, &e); return e; }
-__device__ inline int exp_of(double x) { int e; frexp(x, &e); return e; }
-__device__ inline float scale2(float x, int e) { return ldexpf(x, e); }
-__device__ inline double scale2(double x, int e) { return ldexp(x, e); }
-
 constexpr int PR_THREADS = 256;
 
 template <typename T, int TC>
@@ -427,63 +372,6 @@ struct PruneSmem {
         return (b + 15) & ~size_t(15);
     }
 };
-
-template <typename T, int TC, bool KAHAN>
-__device__ inline void child_partial(const T *Et, const T *slots, int slot, int leaf, const uint8_t *lvT, int a0,
-                                     int c0, T v[4][TC / 16])
-{
-    constexpr int CPT = TC / 16;
-    if (slot < 0) {
-#pragma unroll
-        for (int cc = 0; cc < CPT; cc++) {
-            int s = lvT[leaf * TC + c0 + cc];
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                int a = a0 + i;
-                v[i][cc] = (s >= K) ? (T)1 : (Et[s * K + a] + (a == s ? (T)1 : (T)0));
-            }
-        }
-        return;
-    }
-    const T *al = slots + (size_t)slot * K * TC;
-    // sum_j E[a][j] alpha[j] accumulated separately from alpha[a] (added last)
-    T acc[4][CPT], comp[4][CPT];
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int cc = 0; cc < CPT; cc++) {
-            acc[i][cc] = (T)0;
-            comp[i][cc] = (T)0;
-        }
-#pragma unroll 4
-    for (int j = 0; j < K; j++) {
-        T e[4], x[CPT];
-        Vec4<T>::load(Et + j * K + a0, e);
-        ColLoad<T, CPT>::load(al + j * TC + c0, x);
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-#pragma unroll
-            for (int cc = 0; cc < CPT; cc++) {
-                if (KAHAN) {
-                    // compensated summation: the rounding error of each addition is
-                    // carried in comp, so small terms are not lost against a large sum
-                    T y = e[i] * x[cc] - comp[i][cc];
-                    T t = acc[i][cc] + y;
-                    comp[i][cc] = (t - acc[i][cc]) - y;
-                    acc[i][cc] = t;
-                } else {
-                    acc[i][cc] += e[i] * x[cc];
-                }
-            }
-    }
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        T x[CPT];
-        ColLoad<T, CPT>::load(al + (a0 + i) * TC + c0, x);
-#pragma unroll
-        for (int cc = 0; cc < CPT; cc++) v[i][cc] = x[cc] + (acc[i][cc] - comp[i][cc]);
-    }
-}
 
 template <typename T, int TC, bool KAHAN>
 __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
@@ -603,6 +491,7 @@ __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
 
 int prune_tile_cols(int prec)
 {
+    if (prec == PCSF_PREC_TF32X3 || prec == PCSF_PREC_TF32) return 128;
     return prec == PCSF_PREC_FP64 ? 32 : 64;
 }
 

@@ -103,6 +103,37 @@ cudaError_t launch_prune(int prec, bool compensated, const PruneArgs &a, cudaStr
 int prune_tile_cols(int prec);
 size_t prune_smem_bytes(int prec, int nslots, int nl, int nint);
 
+// Adjoint gradient over work items (grad_kernels.cu): per work item the lpr /
+// elpr partials and d lpr / d t_c for every branch c.
+struct GradArgs {
+    const WorkItem *wi;
+    int nwi;
+    const Request *req;
+    const uint8_t *leaves;
+    const void *Pbuf;
+    const SchedNode *sched;
+    int n_internal;
+    int nl;
+    int nbr;
+    int nslots;
+    DevModels m;
+    const void *Qrow;        // [2][K][K] Q row-major in the arithmetic type
+    void *scratch;           // gridDim.x * scratch_per_cta bytes
+    size_t scratch_per_cta;
+    double *partials;        // [nwi][2]
+    double *gpart;           // [nwi][nbr]
+};
+cudaError_t launch_grad(int prec, bool compensated, const GradArgs &a, cudaStream_t s, int grid);
+size_t grad_scratch_per_cta(int prec, int nl);
+size_t grad_smem_bytes(int prec, int nslots, int nl, int nint);
+cudaError_t launch_reduce_grad(const double *gpart, const int32_t *wi_begin, int nreq, int nbr, double *grad,
+                               cudaStream_t s);
+
+// Tensor-core pruning (tc_kernels.cu): nprod 3 = TF32 hi/lo split, 1 = single TF32.
+cudaError_t launch_prune_tc(int nprod, const PruneArgs &a, int *err, cudaStream_t s, int grid);
+size_t prune_tc_smem_bytes(int nl);
+bool prune_tc_supported(int nslots, int nl);
+
 // Sum the partials of each request's contiguous work items in fixed order.
 cudaError_t launch_reduce(const double *partials, const int32_t *wi_begin, int nreq, double *out_lpr,
                           double *out_elpr, cudaStream_t s);

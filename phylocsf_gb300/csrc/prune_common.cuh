@@ -1,0 +1,140 @@
+// Device helpers shared by the pruning and gradient kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "pcsf_internal.h"
+
+namespace pcsf {
+
+template <typename T> struct Vec4;
+template <> struct Vec4<float> {
+    static __device__ inline void load(const float *p, float v[4])
+    {
+        float4 x = *reinterpret_cast<const float4 *>(p);
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+    }
+};
+template <> struct Vec4<double> {
+    static __device__ inline void load(const double *p, double v[4])
+    {
+        double2 x = *reinterpret_cast<const double2 *>(p);
+        double2 y = *reinterpret_cast<const double2 *>(p + 2);
+        v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
+    }
+};
+
+template <typename T> struct AtomMax;
+template <> struct AtomMax<float> {
+    typedef int U;
+    static __device__ inline void upd(U *p, float v) { atomicMax(p, __float_as_int(v)); }
+    static __device__ inline float get(const U *p) { return __int_as_float(*p); }
+};
+template <> struct AtomMax<double> {
+    typedef unsigned long long U;
+    static __device__ inline void upd(U *p, double v) { atomicMax(p, (unsigned long long)__double_as_longlong(v)); }
+    static __device__ inline double get(const U *p) { return __longlong_as_double((long long)*p); }
+};
+
+template <typename T, int CPT> struct ColLoad;
+template <> struct ColLoad<float, 4> {
+    static __device__ inline void load(const float *p, float v[4]) { Vec4<float>::load(p, v); }
+};
+template <> struct ColLoad<float, 2> {
+    static __device__ inline void load(const float *p, float v[2])
+    {
+        float2 x = *reinterpret_cast<const float2 *>(p);
+        v[0] = x.x; v[1] = x.y;
+    }
+};
+template <> struct ColLoad<double, 2> {
+    static __device__ inline void load(const double *p, double v[2])
+    {
+        double2 x = *reinterpret_cast<const double2 *>(p);
+        v[0] = x.x; v[1] = x.y;
+    }
+};
+template <> struct ColLoad<double, 4> {
+    static __device__ inline void load(const double *p, double v[4]) { Vec4<double>::load(p, v); }
+};
+
+__device__ inline int exp_of(float x) { int e; frexpf(x, &e); return e; }
+__device__ inline int exp_of(double x) { int e; frexp(x, &e); return e; }
+__device__ inline float scale2(float x, int e) { return ldexpf(x, e); }
+__device__ inline double scale2(double x, int e) { return ldexp(x, e); }
+
+// out[i][cc] = sum_j M[j][a0+i] * X[j][c0+cc] for a 64 x TC shared-memory tile
+// X ([K][TC]) and a 64 x 64 matrix M ([K][K], row j contiguous), optionally
+// with compensated summation.
+template <typename T, int TC, bool KAHAN>
+__device__ inline void contract(const T *M, const T *X, int a0, int c0, T out[4][TC / 16])
+{
+    constexpr int CPT = TC / 16;
+    T comp[4][CPT];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int cc = 0; cc < CPT; cc++) {
+            out[i][cc] = (T)0;
+            comp[i][cc] = (T)0;
+        }
+#pragma unroll 4
+    for (int j = 0; j < K; j++) {
+        T e[4], x[CPT];
+        Vec4<T>::load(M + j * K + a0, e);
+        ColLoad<T, CPT>::load(X + j * TC + c0, x);
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int cc = 0; cc < CPT; cc++) {
+                if (KAHAN) {
+                    // compensated summation: the rounding error of each addition is
+                    // carried in comp, so small terms are not lost against a large sum
+                    T y = e[i] * x[cc] - comp[i][cc];
+                    T t = out[i][cc] + y;
+                    comp[i][cc] = (t - out[i][cc]) - y;
+                    out[i][cc] = t;
+                } else {
+                    out[i][cc] += e[i] * x[cc];
+                }
+            }
+    }
+    if (KAHAN) {
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int cc = 0; cc < CPT; cc++) out[i][cc] -= comp[i][cc];
+    }
+}
+
+// Partial of child c at its parent: v[a] = alpha_c[a] + sum_j E_c[a][j] alpha_c[j]
+// (internal child, slot >= 0; Et = E_c^T) or the gather v[a] = P_c[a][s] of a
+// leaf in state s (1 for a marginalised leaf: P rows sum to 1).
+template <typename T, int TC, bool KAHAN>
+__device__ inline void child_partial(const T *Et, const T *slots, int slot, int leaf, const uint8_t *lvT, int a0,
+                                     int c0, T v[4][TC / 16])
+{
+    constexpr int CPT = TC / 16;
+    if (slot < 0) {
+#pragma unroll
+        for (int cc = 0; cc < CPT; cc++) {
+            int s = lvT[leaf * TC + c0 + cc];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                int a = a0 + i;
+                v[i][cc] = (s >= K) ? (T)1 : (Et[s * K + a] + (a == s ? (T)1 : (T)0));
+            }
+        }
+        return;
+    }
+    const T *al = slots + (size_t)slot * K * TC;
+    contract<T, TC, KAHAN>(Et, al, a0, c0, v);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        T x[CPT];
+        ColLoad<T, CPT>::load(al + (a0 + i) * TC + c0, x);
+#pragma unroll
+        for (int cc = 0; cc < CPT; cc++) v[i][cc] = x[cc] + v[i][cc];
+    }
+}
+
+}  // namespace pcsf

@@ -1,0 +1,88 @@
+"""GPU adjoint gradient (pcsf_grad) against the oracle's outside pass and finite differences.
+
+Tolerances: FP64 engine, per-branch d lpr / d t within 1e-8 relative (abs
+floor 1e-8) of the oracle; FP32 (compensated) within 1e-3 relative of the
+largest |gradient| entry.  d lpr / d rho against a central difference of the
+FP64 engine's lpr with h = 1e-5: within 1e-6 relative.
+"""
+import numpy as np
+import pytest
+
+import phylocsf_gb300 as P
+from phylocsf_gb300 import synth
+from oracle import oracle as O
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+_E = {}
+
+
+def engine(name, prec):
+    if (name, prec) not in _E:
+        ps = synth.load_params(name)
+        _E[(name, prec)] = P.Engine(ps.tree, ps.S_c, ps.pi_c, ps.S_n, ps.pi_n, precision=prec)
+    return _E[(name, prec)]
+
+
+def _data(name, lengths, seed):
+    ps = synth.load_params(name)
+    rng = np.random.default_rng(seed)
+    gf = synth.gap_fractions(rng, len(lengths), ps.tree.nl, 0.05, 0.4, 0.2)
+    return synth.simulate(ps, np.asarray(lengths), (np.arange(len(lengths)) % 2).astype(np.int32), gf, seed)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _fast():
+    O.set_sparse_leaves(True)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+@pytest.mark.parametrize("name", ["12flies", "29mammals"])
+def test_branch_gradient_matches_oracle(prec, name):
+    e = engine(name, prec)
+    mc, mn, ot, tree = H.oracle_models(name)
+    offs, leaves = _data(name, [90, 1, 200, 0], seed=21)
+    b = e.batch(offs, leaves)
+    for model, om in ((0, mc), (1, mn)):
+        for rho in (0.3, 1.0, 2.5):
+            lpr, db, drho, st = e.grad(b, model, rho)
+            assert (st == 0).all()
+            for r in range(len(offs) - 1):
+                lv = H.u8_to_oracle(leaves[offs[r]:offs[r + 1]])
+                lo, go = O.grad_branches(om, ot, rho, lv)
+                if lv.shape[0] == 0:
+                    assert np.all(db[r] == 0.0) and lpr[r] == 0.0
+                    continue
+                if prec == "fp64":
+                    assert lpr[r] == pytest.approx(lo, rel=1e-9)
+                    assert np.allclose(db[r], go, rtol=1e-8, atol=1e-8)
+                else:
+                    scale = np.abs(go).max()
+                    assert np.abs(db[r] - go).max() <= 1e-3 * scale + 1e-6, (np.abs(db[r] - go).max(), scale)
+                assert drho[r] == pytest.approx(float(tree.branch[: tree.n - 1] @ db[r]), rel=1e-12, abs=1e-12)
+
+
+def test_rho_gradient_matches_central_difference():
+    e = engine("58mammals", "fp64")
+    offs, leaves = _data("58mammals", [150, 700], seed=3)
+    b = e.batch(offs, leaves)
+    h = 1e-5
+    for model in (0, 1):
+        for rho in (0.5, 1.0, 3.0):
+            _, _, drho, st = e.grad(b, model, rho)
+            fp = e.lpr(b, model, rho + h)[0]
+            fm = e.lpr(b, model, rho - h)[0]
+            fd = (fp - fm) / (2 * h)
+            assert np.allclose(drho, fd, rtol=1e-6, atol=1e-6), (drho, fd)
+
+
+def test_gradient_zero_at_mle():
+    """At the fitted rho the derivative in rho is close to zero (relative to its scale)."""
+    e = engine("29mammals", "fp64")
+    offs, leaves = _data("29mammals", [400], seed=8)
+    res = e.score_batch(offs, leaves, P.MLE)
+    b = e.batch(offs, leaves)
+    _, _, d1, _ = e.grad(b, 0, res[0]["rho_c"])
+    _, _, d2, _ = e.grad(b, 0, res[0]["rho_c"] * 1.2)
+    assert abs(d1[0]) < 0.05 * abs(d2[0])

@@ -1,0 +1,100 @@
+"""Tensor-core (tcgen05, TF32 hi/lo split) pruning against the FP64 oracle and the FP64 GPU path.
+
+Tolerances: tf32x3 lpr within 2.3e-4 nats (= 1e-3 dB) per model on regions up
+to 3000 codons for rho in [0.1, 10]; mle scores within 1e-3 dB of the FP64
+path for >= 95% of regions and within 5e-3 dB for all.  The single-product
+tf32 mode is a precision-study mode: only its relative lpr error (< 1e-3) is
+checked.
+"""
+import numpy as np
+import pytest
+
+import phylocsf_gb300 as P
+from phylocsf_gb300 import driver as D
+from phylocsf_gb300 import synth
+from oracle import oracle as O
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+_E = {}
+
+
+def engine(name, prec):
+    if (name, prec) not in _E:
+        ps = synth.load_params(name)
+        _E[(name, prec)] = P.Engine(ps.tree, ps.S_c, ps.pi_c, ps.S_n, ps.pi_n, precision=prec)
+    return _E[(name, prec)]
+
+
+def _data(name, lengths, seed):
+    ps = synth.load_params(name)
+    rng = np.random.default_rng(seed)
+    gf = synth.gap_fractions(rng, len(lengths), ps.tree.nl, 0.05, 0.4, 0.2)
+    return synth.simulate(ps, np.asarray(lengths), (np.arange(len(lengths)) % 2).astype(np.int32), gf, seed)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _fast():
+    O.set_sparse_leaves(True)
+
+
+@pytest.mark.parametrize("name,lengths", [("12flies", [300, 1, 127, 128, 129, 0, 7]),
+                                          ("58mammals", [50, 333, 1000, 3000])])
+def test_tf32x3_lpr_matches_oracle(name, lengths):
+    e = engine(name, "tf32x3")
+    mc, mn, ot, tree = H.oracle_models(name)
+    offs, leaves = _data(name, lengths, seed=11)
+    b = e.batch(offs, leaves)
+    for model, om in ((0, mc), (1, mn)):
+        for rho in (0.1, 1.0, 3.3, 10.0):
+            lpr, elpr, st = e.lpr(b, model, rho)
+            assert (st == 0).all()
+            for r in range(len(lengths)):
+                lo, eo = O.lpr_leaves(om, ot, rho, H.u8_to_oracle(leaves[offs[r]:offs[r + 1]]))
+                assert abs(lpr[r] - lo) <= 2.3e-4, (r, rho, lpr[r] - lo)
+                assert abs(elpr[r] - eo) <= 2.3e-4, (r, rho, elpr[r] - eo)
+
+
+def test_tf32_single_product_runs():
+    e = engine("58mammals", "tf32")
+    mc, mn, ot, tree = H.oracle_models("58mammals")
+    offs, leaves = _data("58mammals", [200, 500], seed=3)
+    lpr, _, st = e.lpr(e.batch(offs, leaves), 0, 1.0)
+    assert (st == 0).all()
+    for r in range(2):
+        lo, _ = O.lpr_leaves(mc, ot, 1.0, H.u8_to_oracle(leaves[offs[r]:offs[r + 1]]))
+        assert abs(lpr[r] - lo) <= 1e-3 * abs(lo)
+
+
+def test_tf32x3_mle_close_to_fp64():
+    offs, leaves = _data("58mammals", list(np.random.default_rng(2).integers(50, 1500, size=64)), seed=2)
+    a = engine("58mammals", "fp64").score_batch(offs, leaves, P.MLE)
+    b = engine("58mammals", "tf32x3").score_batch(offs, leaves, P.MLE)
+    assert (b["status"] == 0).all()
+    d = np.abs(a["score"] - b["score"])
+    assert (d <= 1e-3).mean() >= 0.95, np.sort(d)[-8:]
+    assert d.max() <= 5e-3, np.sort(d)[-8:]
+
+
+@pytest.mark.parametrize("idx", [0, 1, 2, 3])
+def test_tf32x3_reference_pins(idx):
+    p = H.pins()[idx]
+    f = H.parse_flags(p["flags"])
+    e = engine(p["params"], "tf32x3")
+    ex = H.examples()[p["file"]]
+    mfa = "\n".join(">%s\n%s" % (s, r) for s, r in zip(ex["species"], ex["rows"])) + "\n"
+    opts = D.Options(strategy=P.MLE, frames=f["frames"], orf_mode=f["orf"], remove_ref_gaps=f["remove_ref_gaps"],
+                     anc_comp=True, aa=f["aa"])
+    best = D.process_alignment(e, mfa, opts).best
+    assert p["windows"][0][0] < best.result["score"] < p["windows"][0][1]
+    if p["ints"]:
+        assert [best.lo, best.hi] == p["ints"]
+
+
+def test_tf32x3_deterministic():
+    e = engine("58mammals", "tf32x3")
+    offs, leaves = _data("58mammals", [500, 70, 1200], seed=9)
+    a = e.score_batch(offs, leaves, P.MLE)
+    b = e.score_batch(offs, leaves, P.MLE)
+    assert a.tobytes() == b.tobytes()
