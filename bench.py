@@ -182,6 +182,15 @@ def run_reference(args, world, rank):
 
 # ---------------------------------------------------------------- our arm
 def make_workload(args, seed):
+    wl = _make_workload(args, seed)
+    if args.strategy is not None:
+        import phylocsf_gb300 as P
+        wl.strategy = P.FIXED if args.strategy == "fixed" else P.MLE
+        wl.name = wl.name.replace("_mle", "_" + args.strategy).replace("_fixed", "_" + args.strategy)
+    return wl
+
+
+def _make_workload(args, seed):
     from phylocsf_gb300 import synth
     if args.workload == "58mammals_mle":
         return synth.workload_58mammals_mle(n_regions=args.regions, seed=seed)
@@ -345,6 +354,8 @@ def main():
     ap.add_argument("--regions", type=int, default=10000)
     ap.add_argument("--cols", type=int, default=2_000_000)
     ap.add_argument("--precision", default="fp32c")
+    ap.add_argument("--strategy", default=None, choices=[None, "fixed", "mle"],
+                    help="override the workload's strategy (fixed: one likelihood pass, used for profiling)")
     ap.add_argument("--fp64-regions", type=int, default=256)
     ap.add_argument("--cpu-cores", type=int, default=0)
     ap.add_argument("--no-accuracy", action="store_true")

@@ -5,8 +5,9 @@ Tolerances (stated per test):
     within 1e-6 dB (same Brent iterates as the oracle).
   - FP32 engines (FP32 contractions on P-I, FP64 eigensystem / exp / sums,
     P(t) corrected around an FP64 grid): P(t) entries within 2e-6.
-    fp32c (compensated summation): |d lpr| within 2.3e-4 nats (= 1e-3 dB) per
-    model on regions up to 3000 codons for rho in [0.1, 10], fixed-strategy
+    fp32c (compensated summation): |d lpr| within max(2.3e-4 nats (= 1e-3 dB),
+    5e-9 |lpr|) per model on regions up to 3000 codons for rho in [0.1, 10]
+    (the relative term only matters far from the optimum, e.g. rho = 10), fixed-strategy
     |d score| <= 1e-3 dB.  fp32 (plain summation) carries a downward bias of
     ~0.3 ulp per contraction; its lpr tolerance is 4e-3 nats.
 """
@@ -98,7 +99,7 @@ def test_lpr_matches_oracle(prec, name, lengths):
                     assert lpr[r] == pytest.approx(lo, rel=1e-9, abs=1e-9)
                     assert elpr[r] == pytest.approx(eo, rel=1e-9, abs=1e-9)
                 else:
-                    tol = 2.3e-4 if prec == "fp32c" else 4e-3
+                    tol = max(2.3e-4, 5e-9 * abs(lo)) if prec == "fp32c" else 4e-3
                     assert abs(lpr[r] - lo) <= tol, (r, rho, lpr[r] - lo)
                     assert abs(elpr[r] - eo) <= tol, (r, rho, elpr[r] - eo)
 
