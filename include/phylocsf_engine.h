@@ -59,6 +59,10 @@ extern "C" {
  * below half an ulp, a bias that accumulates over thousands of columns. */
 #define PCSF_COMPENSATED (1 << 16)
 
+/* engine flag for the tensor-core modes: pcsf_lpr returns the tensor-core
+ * kernel's values instead of the compensated FP32 kernel's (precision study). */
+#define PCSF_TC_DIRECT (1 << 17)
+
 /* engine flags, bits 8..15: CUDA device ordinal + 1 (0 = the calling thread's
  * current device).  Every call on an engine runs on the engine's device. */
 #define PCSF_DEVICE(d) ((((int32_t)(d)) + 1) << 8)
@@ -124,6 +128,10 @@ int pcsf_engine_create_q(const pcsf_tree *tree, const double *Q_c, const double 
                          const double *Q_n, const double *eq_n, const double *prior_n, int32_t flags,
                          pcsf_engine **out);
 
+/* Create an engine for one tree without fixed models, for the OmegaModel test
+ * (pcsf_omega_score), whose rate matrices change with every kappa. */
+int pcsf_engine_create_tree(const pcsf_tree *tree, int32_t flags, pcsf_engine **out);
+
 void pcsf_engine_destroy(pcsf_engine *e);
 
 /* Last error message of this engine (static storage if e == NULL). */
@@ -180,6 +188,26 @@ int pcsf_lpr(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, do
  * sense of an autograd.Function. */
 int pcsf_grad(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, double *lpr, double *d_branch,
               double *d_rho, int32_t *status);
+
+/* ------------------------------------------------------------ OmegaModel */
+
+/* One region's dN/dS test (OmegaModel.score, src/OmegaModel.ml:195-219). */
+typedef struct {
+    double score;               /* decibans, 10*(lpr_H1 - lpr_H0)/ln 10           */
+    double lpr_h0, lpr_h1;      /* log posterior at the fitted kappa (prior included) */
+    double rho_h0, kappa_h0;    /* H0 (omega = sigma = 1) estimates                */
+    double rho_h1, kappa_h1;    /* H1 (omega = omega_h1, sigma = sigma_h1)          */
+    int32_t status;
+    int32_t evals;
+} pcsf_omega_result;
+
+/* The OmegaModel test for every region of a batch: F3x4 codon frequencies from
+ * the region's leaves (OmegaModel.ml:102-134), then for H0 and H1 three rounds
+ * of rho (half-Cauchy prior) and kappa (Gamma prior) maximisation
+ * (kr_map, OmegaModel.ml:160-190).  Every kappa change is a new rate matrix,
+ * eigendecomposed in FP64 on the GPU; its P(t) is formed in FP64.  The
+ * reference defaults are omega_h1 = 0.2, sigma_h1 = 0.01. */
+int pcsf_omega_score(pcsf_engine *e, pcsf_batch *b, double omega_h1, double sigma_h1, pcsf_omega_result *out);
 
 #ifdef __cplusplus
 }

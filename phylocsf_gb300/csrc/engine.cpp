@@ -16,6 +16,7 @@
 // exact rho, so repeated evaluations at the same point (which the reference
 // performs and which give bit-identical results) are not recomputed.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -100,6 +101,8 @@ struct pcsf_engine {
     cudaEvent_t ev[8] = {};
     int prec = PCSF_PREC_FP32;
     bool compensated = false;
+    bool tc_direct = false;
+    bool has_models = false;
     std::string err;
 
     // tree
@@ -123,6 +126,7 @@ struct pcsf_engine {
 
     // per-launch work buffers
     DevBuf<unsigned char> Pbuf;
+    DevBuf<double> Pbuf64;
     size_t pbuf_psets = 0;
     DevBuf<PSet> dps;
     DevBuf<Request> dreq;
@@ -421,6 +425,7 @@ static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2],
     e->dm.wlog = e->dwlog.p;
     e->dm.tol = e->tol;
     e->dm.grid_n = 0;
+    e->has_models = true;
     {
         // Q row-major in both arithmetic types, for dP/dt = Q P(t) in the gradient
         std::vector<double> qd(2 * K2);
@@ -450,6 +455,7 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
         return e->fail(PCSF_EINVAL, "precision mode %d is not available in this build", prec);
     e->prec = prec;
     e->compensated = (flags & PCSF_COMPENSATED) != 0;
+    e->tc_direct = (flags & PCSF_TC_DIRECT) != 0;
     int ndev = 0;
     cudaError_t ce = cudaGetDeviceCount(&ndev);
     if (ce != cudaSuccess || ndev == 0)
@@ -511,15 +517,24 @@ struct Eval {
 };
 
 // grad (optional): d lpr / d t_c per request, [nreq][nbr], by the adjoint kernel.
+// accurate: on a tensor-core engine, use the compensated FP32 kernel instead
+// (every likelihood the engine returns comes from it; see tc_kernels.cu).
+// dyn: per-request models (Request.model indexes this table) instead of the
+// engine's two fixed models; their P(t) is formed in FP64 (no FP32 grid exists
+// for them) and the pruning runs on the SIMT kernels.
 static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &reqs_in, std::vector<Eval> &out,
-                    std::vector<double> *grad = nullptr)
+                    std::vector<double> *grad = nullptr, bool accurate = false, const DevModels *dyn = nullptr)
 {
     const int nreq = (int)reqs_in.size();
     out.assign(nreq, Eval{0.0, 0.0, PCSF_OK});
     if (nreq == 0) return PCSF_OK;
-    const bool tc = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
+    if (dyn && grad) return e->fail(PCSF_EINVAL, "gradients are not available for per-request models");
+    if (dyn) accurate = true;
+    const DevModels dmv = dyn ? *dyn : e->dm;
+    const bool tc = (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32) && !accurate;
     // the gradient always runs the SIMT adjoint kernel (64-column tiles in FP32)
-    const int TC = grad ? (e->prec == PCSF_PREC_FP64 ? 32 : 64) : prune_tile_cols(e->prec);
+    const int TC = (grad || !tc) ? (e->prec == PCSF_PREC_FP64 ? 32 : 64) : prune_tile_cols(e->prec);
+    const bool simt_comp = e->compensated || accurate;
 
     // work items, P-set dedup and chunking (at most pbuf_psets distinct P sets per chunk)
     std::vector<Request> reqs(reqs_in);
@@ -588,6 +603,8 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     for (size_t c = 0; c + 1 < chunk_ps_begin.size(); c++)
         max_chunk_ps = std::max<size_t>(max_chunk_ps, chunk_ps_begin[c + 1] - chunk_ps_begin[c]);
     CK(e->Pbuf.reserve(max_chunk_ps * pset_bytes), "cudaMalloc P(t) buffer");
+    const bool stage64 = dyn && e->prec != PCSF_PREC_FP64;   // FP64 formation, then FP32 storage
+    if (stage64) CK(e->Pbuf64.reserve(max_chunk_ps * (size_t)e->nbr * K2), "cudaMalloc P(t) staging buffer");
     size_t gscr = 0;
     if (grad) {
         gscr = grad_scratch_per_cta(e->prec, e->nl);
@@ -614,8 +631,16 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         int r0 = chunk_req_begin[c], r1 = chunk_req_begin[c + 1];
         int p0 = chunk_ps_begin[c], p1 = chunk_ps_begin[c + 1];
         CK(cudaEventRecord(e->ev[0], s), "event");
-        CK(launch_pform(e->prec == PCSF_PREC_FP64, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, e->dm, e->Pbuf.p,
-                        e->dstatus.p + p0, s), "P(t) formation launch");
+        if (stage64) {
+            CK(launch_pform(true, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, dmv, e->Pbuf64.p, e->dstatus.p + p0, s),
+               "P(t) formation launch");
+            CK(launch_d2f(e->Pbuf64.p, reinterpret_cast<float *>(e->Pbuf.p), (size_t)(p1 - p0) * e->nbr * K2, s),
+               "P(t) conversion launch");
+            e->stats.kernel_launches += 1;
+        } else {
+            CK(launch_pform(e->prec == PCSF_PREC_FP64 || dyn, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, dmv,
+                            e->Pbuf.p, e->dstatus.p + p0, s), "P(t) formation launch");
+        }
         CK(cudaEventRecord(e->ev[1], s), "event");
         PruneArgs pa{};
         pa.wi = e->dwi.p + wib[r0];
@@ -628,7 +653,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         pa.nl = e->nl;
         pa.nbr = e->nbr;
         pa.nslots = e->nslots;
-        pa.m = e->dm;
+        pa.m = dmv;
         pa.partials = e->dpart.p + 2 * (size_t)wib[r0];
         if (grad) {
             GradArgs ga{};
@@ -656,7 +681,8 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
             CK(launch_prune_tc(e->prec == PCSF_PREC_TF32X3 ? 3 : 1, pa, e->derr.p, s, grid), "tensor-core pruning launch");
         } else {
             int grid = std::min(e->prune_grid, std::max(pa.nwi, 1));
-            CK(launch_prune(e->prec, e->compensated, pa, s, grid), "pruning launch");
+            CK(launch_prune(e->prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32, simt_comp, pa, s, grid),
+               "pruning launch");
         }
         CK(cudaEventRecord(e->ev[2], s), "event");
         e->stats.pform_launches += (p1 > p0);
@@ -714,6 +740,9 @@ struct Fit {
     int region = 0, model = 0;
     int64_t ncols = 0;
     bool deriv = false;   // derivative-assisted small steps (reduced precision)
+    bool accurate_final = false;   // report f(x) from the compensated kernel (tensor-core engines)
+    int prior_kind = 0;            // OmegaModel objectives add a prior on the variable (0: none)
+    std::deque<std::pair<double, Eval>> acache;     // rho -> accurate evaluation
     std::deque<std::pair<double, double>> gcache;   // rho -> d lpr / d rho
     double lo = 1e-2, hi = 10.0, init = 1.0, accuracy = 0.01;
     int maxtries = 250;
@@ -745,15 +774,17 @@ struct Fit {
     }
 };
 
-// Advance until a value outside the cache is needed (appended to `need`, or to
-// `need_grad` for a gradient) or done.
-static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need_grad)
+// Advance until a value outside the cache is needed (appended to `need`, to
+// `need_grad` for a gradient, or to `need_acc` for an accurate evaluation) or done.
+static double prior_value(int kind, double x);
+
+static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need_grad, std::vector<double> &need_acc)
 {
     auto ask = [&](double r) -> const Eval * {
         const Eval *ev = f.get(r);
         if (ev) return ev;
-        if (f.ncols == 0) {   // empty region: the objective is identically 0
-            f.cache.push_back({r, Eval{0.0, 0.0, PCSF_OK}});
+        if (f.ncols == 0) {   // empty region: the likelihood term is identically 0
+            f.cache.push_back({r, Eval{prior_value(f.prior_kind, r), 0.0, PCSF_OK}});
             return &f.cache.back().second;
         }
         need.push_back(r);
@@ -917,8 +948,18 @@ static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need
             break;
         }
         case Fit::FINAL: {
-            const Eval *a = ask(f.x);
-            if (!a) return;
+            const Eval *a = nullptr;
+            if (f.accurate_final && f.ncols > 0) {
+                for (auto &c : f.acache)
+                    if (c.first == f.x) a = &c.second;
+                if (!a) {
+                    need_acc.push_back(f.x);
+                    return;
+                }
+            } else {
+                a = ask(f.x);
+                if (!a) return;
+            }
             if (failed(a)) return;
             f.rho = f.x;
             f.lpr = a->lpr;
@@ -939,25 +980,28 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
     // PCSF_TRACE_REGION=<r>: print every evaluation of region r's fits to stderr
     const char *tr = std::getenv("PCSF_TRACE_REGION");
     const int trace = tr ? std::atoi(tr) : -1;
-    std::vector<Request> reqs, greqs;
-    std::vector<std::pair<int, double>> owner, gowner;
-    std::vector<Eval> res, gres;
+    std::vector<Request> reqs, greqs, areqs;
+    std::vector<std::pair<int, double>> owner, gowner, aowner;
+    std::vector<Eval> res, gres, ares;
     std::vector<double> grad;
     for (;;) {
         reqs.clear();
         owner.clear();
         greqs.clear();
         gowner.clear();
+        areqs.clear();
+        aowner.clear();
         for (int i = 0; i < (int)fits.size(); i++) {
-            std::vector<double> need, needg;
-            advance(fits[i], need, needg);
-            for (auto *lst : {&need, &needg}) {
+            std::vector<double> need, needg, needa;
+            advance(fits[i], need, needg, needa);
+            for (auto *lst : {&need, &needg, &needa}) {
                 std::sort(lst->begin(), lst->end());
                 lst->erase(std::unique(lst->begin(), lst->end()), lst->end());
             }
             bool bad = false;
             for (double r : need) bad |= !(r > 0.0) || !std::isfinite(r);
             for (double r : needg) bad |= !(r > 0.0) || !std::isfinite(r);
+            for (double r : needa) bad |= !(r > 0.0) || !std::isfinite(r);
             if (bad) {
                 fits[i].status = PCSF_EINVAL;
                 fits[i].phase = Fit::DONE;
@@ -979,8 +1023,16 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
                 greqs.push_back(q);
                 gowner.push_back({i, r});
             }
+            for (double r : needa) {
+                Request q{};
+                q.region = fits[i].region;
+                q.model = fits[i].model;
+                q.rho = r;
+                areqs.push_back(q);
+                aowner.push_back({i, r});
+            }
         }
-        if (reqs.empty() && greqs.empty()) break;
+        if (reqs.empty() && greqs.empty() && areqs.empty()) break;
         e->stats.rounds += 1;
         if (!reqs.empty()) {
             int rc = evaluate(e, b, reqs, res);
@@ -990,6 +1042,11 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
             int rc = evaluate(e, b, greqs, gres, &grad);
             if (rc) return rc;
         }
+        if (!areqs.empty()) {
+            int rc = evaluate(e, b, areqs, ares, nullptr, true);
+            if (rc) return rc;
+        }
+        for (size_t k = 0; k < areqs.size(); k++) fits[aowner[k].first].acache.push_back({aowner[k].second, ares[k]});
         for (size_t k = 0; k < reqs.size(); k++) {
             Fit &f = fits[owner[k].first];
             f.cache.push_back({owner[k].second, res[k]});
@@ -1025,6 +1082,7 @@ static int score_impl(pcsf_engine *e, pcsf_batch *b, int strategy, pcsf_result *
             f.model = m;
             f.ncols = b->offs[r + 1] - b->offs[r];
             f.deriv = e->prec != PCSF_PREC_FP64;
+            f.accurate_final = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
             if (strategy == PCSF_FIXED) {
                 // llr_FixedLik 1.0: a single evaluation at rho = 1
                 f.x = 1.0;
@@ -1046,7 +1104,370 @@ static int score_impl(pcsf_engine *e, pcsf_batch *b, int strategy, pcsf_result *
         o.elpr_n = nf.elpr;
         o.score = decibans(c.lpr - nf.lpr);
         o.anc_comp_score = decibans(c.elpr - nf.elpr);
-        o.evals = (int32_t)(c.cache.size() + nf.cache.size() + c.gcache.size() + nf.gcache.size());
+        o.evals = (int32_t)(c.cache.size() + nf.cache.size() + c.gcache.size() + nf.gcache.size() + c.acache.size() +
+                            nf.acache.size());
+    }
+    return PCSF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// OmegaModel (src/OmegaModel.ml): parametric codon Q, priors, and the H0/H1
+// maximum-a-posteriori fits of rho and kappa.
+
+typedef std::array<double, 12> OmegaKey;   // kappa, omega, sigma, F3x4 (A, C, G relative to T) x 3 positions
+
+// pi_exprs (OmegaModel.ml:21-40) and the rate matrix q_p14n / q_scale (:42-80).
+static void omega_q(const OmegaKey &q, double *Q, double *pi)
+{
+    static const char *aa = "KNKNTTTTRSRSIIMIQHQHPPPPRRRRLLLLEDEDAAAAGGGGVVVV*Y*YSSSS*CWCLFLF";
+    auto nuc = [](int i, int pos) { return pos == 0 ? i / 16 : pos == 1 ? (i / 4) % 4 : i % 4; };
+    auto sc = [&](int i) {
+        double out = 1.0;
+        for (int pos = 0; pos < 3; pos++) {
+            const int n = nuc(i, pos), base = 3 + 3 * pos;
+            const double num = (n == 3) ? 1.0 : q[base + n];
+            const double den = q[base] + (q[base + 1] + (q[base + 2] + 1.0));
+            out *= num / den;
+        }
+        return out;
+    };
+    const double denom = 1.0 - (1.0 - q[2]) * (sc(48) + (sc(50) + sc(56)));
+    for (int i = 0; i < K; i++) pi[i] = sc(i) / denom;
+    auto is_stop = [](int i) { return i == 48 || i == 50 || i == 56; };
+    for (int i = 0; i < K; i++) {
+        double tot = 0.0;
+        for (int j = 0; j < K; j++) {
+            double v = 0.0;
+            if (i != j) {
+                int nd = 0, a = 0, b = 0;
+                for (int pos = 0; pos < 3; pos++)
+                    if (nuc(i, pos) != nuc(j, pos)) { nd++; a = nuc(i, pos); b = nuc(j, pos); }
+                if (nd == 1) {
+                    const bool transition = (a + b == 2 && a != 1 && b != 1) || (a + b == 4 && a != 2 && b != 2);
+                    const double kp = transition ? q[0] : 1.0;
+                    const double op = (!is_stop(i) && !is_stop(j) && aa[i] != aa[j]) ? q[1] : 1.0;
+                    v = pi[j] * (kp * op);
+                }
+            }
+            Q[i * K + j] = v;
+            if (i != j) tot = v + tot;
+        }
+        Q[i * K + i] = 0.0 - tot;
+    }
+    double scale = 0.0;
+    for (int i = 0; i < K; i++) scale = scale - pi[i] * Q[i * K + i];
+    for (int i = 0; i < K2; i++) Q[i] = Q[i] / scale;
+}
+
+// half_cauchy_lpdf ~mode:1 ~scale:0.5 (OmegaModel.ml:148-156) and the Gamma(7, 0.25)
+// density of kappa - 1 (OmegaModel.ml:157; GSL gamma_pdf with shape a, scale b).
+static double prior_value(int kind, double x)
+{
+    if (kind == 1) {
+        const double PI = std::acos(-1.0), mode = 1.0, scale = 0.5;
+        const double numer = 1.0 / (PI * scale * (1.0 + std::pow((x - mode) / scale, 2.0)));
+        const double cdf = std::atan((0.0 - mode) / scale) / PI + 0.5;
+        return std::log(numer) - std::log(1.0 - cdf);
+    }
+    if (kind == 2) {
+        const double y = x - 1.0 + 2.220446049250313e-16, a = 7.0, b = 0.25;
+        if (!(y > 0.0)) return -INFINITY;
+        return (a - 1.0) * std::log(y) - y / b - std::lgamma(a) - a * std::log(b);
+    }
+    return 0.0;
+}
+
+// Eigensystems of per-request models, cached by parameter vector, and the
+// device table of the models a round needs.
+struct DynModels {
+    std::map<OmegaKey, int> index;                  // key -> cache slot
+    std::vector<std::vector<double>> U, lam, eq;    // host cache
+    DevBuf<double> dU, dlam, dsq, disq, dwrow, dprior, dwlog;
+    DevBuf<float> dUf;
+    DevModels dm{};
+};
+
+static int dyn_prepare(pcsf_engine *e, DynModels &dmod, const std::vector<OmegaKey> &keys, std::vector<int> &slot)
+{
+    // eigendecompose the models not seen before, in one batched launch
+    std::vector<int> fresh;
+    slot.resize(keys.size());
+    for (size_t i = 0; i < keys.size(); i++) {
+        auto it = dmod.index.find(keys[i]);
+        if (it == dmod.index.end()) {
+            int id = (int)dmod.U.size();
+            dmod.index[keys[i]] = id;
+            dmod.U.emplace_back(K2);
+            dmod.lam.emplace_back(K);
+            dmod.eq.emplace_back(K);
+            fresh.push_back((int)i);
+            slot[i] = id;
+        } else {
+            slot[i] = it->second;
+        }
+    }
+    if (!fresh.empty()) {
+        const int nf = (int)fresh.size();
+        std::vector<double> A((size_t)nf * K2), Q(K2), pi(K);
+        for (int f = 0; f < nf; f++) {
+            omega_q(keys[fresh[f]], Q.data(), pi.data());
+            std::vector<double> &eqv = dmod.eq[slot[fresh[f]]];
+            for (int i = 0; i < K; i++) eqv[i] = pi[i];
+            for (int i = 0; i < K; i++)
+                for (int j = 0; j < K; j++) {
+                    const double aij = std::sqrt(pi[i]) * Q[i * K + j] / std::sqrt(pi[j]);
+                    const double aji = std::sqrt(pi[j]) * Q[j * K + i] / std::sqrt(pi[i]);
+                    A[(size_t)f * K2 + i * K + j] = 0.5 * (aij + aji);
+                }
+        }
+        DevBuf<double> dA, dUo, dlo;
+        DevBuf<int> dst;
+        CK(dA.reserve((size_t)nf * K2), "cudaMalloc");
+        CK(dUo.reserve((size_t)nf * K2), "cudaMalloc");
+        CK(dlo.reserve((size_t)nf * K), "cudaMalloc");
+        CK(dst.reserve(nf), "cudaMalloc");
+        CK(cudaMemcpyAsync(dA.p, A.data(), sizeof(double) * nf * K2, cudaMemcpyHostToDevice, e->stream), "H2D");
+        CK(launch_jacobi(dA.p, dUo.p, dlo.p, dst.p, nf, e->stream), "eigensolver launch");
+        e->stats.kernel_launches += 1;
+        std::vector<double> Uh((size_t)nf * K2), lh((size_t)nf * K);
+        std::vector<int> sth(nf);
+        CK(cudaMemcpyAsync(Uh.data(), dUo.p, sizeof(double) * nf * K2, cudaMemcpyDeviceToHost, e->stream), "D2H");
+        CK(cudaMemcpyAsync(lh.data(), dlo.p, sizeof(double) * nf * K, cudaMemcpyDeviceToHost, e->stream), "D2H");
+        CK(cudaMemcpyAsync(sth.data(), dst.p, sizeof(int) * nf, cudaMemcpyDeviceToHost, e->stream), "D2H");
+        CK(cudaStreamSynchronize(e->stream), "eigensolver");
+        for (int f = 0; f < nf; f++) {
+            if (sth[f]) return e->fail(PCSF_EEIG, "eigensolver did not converge for an OmegaModel rate matrix");
+            std::copy(Uh.begin() + (size_t)f * K2, Uh.begin() + (size_t)(f + 1) * K2, dmod.U[slot[fresh[f]]].begin());
+            std::copy(lh.begin() + (size_t)f * K, lh.begin() + (size_t)(f + 1) * K, dmod.lam[slot[fresh[f]]].begin());
+        }
+    }
+    // device table for this round: model m of the round = keys[m]
+    const int M = (int)keys.size();
+    std::vector<double> U((size_t)M * K2), lam((size_t)M * K), sq((size_t)M * K), isq((size_t)M * K),
+        wrow((size_t)M * K), prior((size_t)M * K), wlog((size_t)M * K);
+    std::vector<float> Uf((size_t)M * K2);
+    for (int m = 0; m < M; m++) {
+        const int id = slot[m];
+        const std::vector<double> &eqv = dmod.eq[id];
+        double tot = 0.0;
+        for (int i = 0; i < K; i++) tot += eqv[i];
+        for (int i = 0; i < K; i++) {
+            sq[(size_t)m * K + i] = std::sqrt(eqv[i]);
+            isq[(size_t)m * K + i] = 1.0 / std::sqrt(eqv[i]);
+            prior[(size_t)m * K + i] = eqv[i] / tot;     // the equilibrium, normalised (PhyloModel.ml:25-29)
+            wlog[(size_t)m * K + i] = prior[(size_t)m * K + i] * std::log(prior[(size_t)m * K + i]);
+            lam[(size_t)m * K + i] = dmod.lam[id][i];
+        }
+        for (int i = 0; i < K2; i++) {
+            U[(size_t)m * K2 + i] = dmod.U[id][i];
+            Uf[(size_t)m * K2 + i] = (float)dmod.U[id][i];
+        }
+        const double nrm = std::sqrt(tot);
+        for (int mm = 0; mm < K; mm++) {
+            double w = 0.0;
+            for (int j = 0; j < K; j++) w += dmod.U[id][j * K + mm] * sq[(size_t)m * K + j];
+            wrow[(size_t)m * K + mm] = (std::fabs(w) > 1e-9 * nrm) ? w : 0.0;
+        }
+    }
+    CK(dmod.dU.reserve((size_t)M * K2), "cudaMalloc");
+    CK(dmod.dUf.reserve((size_t)M * K2), "cudaMalloc");
+    for (auto *bp : {&dmod.dlam, &dmod.dsq, &dmod.disq, &dmod.dwrow, &dmod.dprior, &dmod.dwlog})
+        CK(bp->reserve((size_t)M * K), "cudaMalloc");
+    CK(cudaMemcpyAsync(dmod.dU.p, U.data(), sizeof(double) * M * K2, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(dmod.dUf.p, Uf.data(), sizeof(float) * M * K2, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(dmod.dlam.p, lam.data(), sizeof(double) * M * K, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(dmod.dsq.p, sq.data(), sizeof(double) * M * K, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(dmod.disq.p, isq.data(), sizeof(double) * M * K, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(dmod.dwrow.p, wrow.data(), sizeof(double) * M * K, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(dmod.dprior.p, prior.data(), sizeof(double) * M * K, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(dmod.dwlog.p, wlog.data(), sizeof(double) * M * K, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaStreamSynchronize(e->stream), "model upload");
+    dmod.dm = DevModels{};
+    dmod.dm.U = dmod.dU.p;
+    dmod.dm.Uf = dmod.dUf.p;
+    dmod.dm.lam = dmod.dlam.p;
+    dmod.dm.sq = dmod.dsq.p;
+    dmod.dm.isq = dmod.disq.p;
+    dmod.dm.wrow = dmod.dwrow.p;
+    dmod.dm.prior = dmod.dprior.p;
+    dmod.dm.wlog = dmod.dwlog.p;
+    dmod.dm.tol = e->tol;
+    dmod.dm.grid_n = 0;
+    return PCSF_OK;
+}
+
+struct OmegaRegion {
+    int region = 0;
+    int64_t ncols = 0;
+    int hyp = 0, round = 0, stage = 0;   // stage 0: rho, 1: kappa
+    OmegaKey q{};
+    double rho = 1.0, lpr_last = 0.0;
+    double lpr_h0 = 0.0, rho_h0 = 0.0, kappa_h0 = 0.0;
+    bool done = false;
+    int status = PCSF_OK, evals = 0;
+    Fit fit;
+
+    void start_fit()
+    {
+        fit = Fit{};
+        fit.region = region;
+        fit.ncols = ncols;
+        fit.accuracy = 0.01;
+        if (stage == 0) {           // kr_map: rho in [0.001, 10] from the current rho
+            fit.lo = 0.001;
+            fit.hi = 10.0;
+            fit.init = rho;
+            fit.prior_kind = 1;
+        } else {                    // kappa in [1, 10] from the current kappa
+            fit.lo = 1.0;
+            fit.hi = 10.0;
+            fit.init = q[0];
+            fit.prior_kind = 2;
+        }
+    }
+};
+
+static int omega_impl(pcsf_engine *e, pcsf_batch *b, double omega_h1, double sigma_h1, pcsf_omega_result *out)
+{
+    const int nreg = b->nreg;
+    std::vector<OmegaRegion> regs(nreg);
+    for (int r = 0; r < nreg; r++) {
+        OmegaRegion &R = regs[r];
+        R.region = r;
+        R.ncols = b->offs[r + 1] - b->offs[r];
+        // new_instance ~kappa:2.5 (omega = sigma = 1), then update_f3x4 from the leaves (OmegaModel.ml:95-134)
+        R.q[0] = 2.5;
+        R.q[1] = 1.0;
+        R.q[2] = 1.0;
+        R.start_fit();
+    }
+    // F3x4 counts need the leaves on the host
+    {
+        std::vector<uint8_t> lv((size_t)b->total_cols * e->nl);
+        if (!lv.empty())
+            CK(cudaMemcpy(lv.data(), b->dleaves.p, lv.size(), cudaMemcpyDeviceToHost), "D2H leaves");
+        for (int r = 0; r < nreg; r++) {
+            double counts[3][4];
+            for (auto &row : counts)
+                for (double &c : row) c = 1.0;
+            for (size_t i = (size_t)b->offs[r] * e->nl; i < (size_t)b->offs[r + 1] * e->nl; i++) {
+                const int c = lv[i];
+                if (c >= K) continue;
+                counts[0][c / 16] += 1.0;
+                counts[1][(c / 4) % 4] += 1.0;
+                counts[2][c % 4] += 1.0;
+            }
+            for (int pos = 0; pos < 3; pos++)
+                for (int n = 0; n < 3; n++) regs[r].q[3 + 3 * pos + n] = counts[pos][n] / counts[pos][3];
+        }
+    }
+    DynModels dmod;
+    std::vector<Request> reqs;
+    std::vector<std::pair<int, double>> owner;
+    std::vector<OmegaKey> keys;
+    std::map<OmegaKey, int> kidx;
+    std::vector<int> slot;
+    std::vector<Eval> res;
+    for (;;) {
+        reqs.clear();
+        owner.clear();
+        keys.clear();
+        kidx.clear();
+        for (int r = 0; r < nreg; r++) {
+            OmegaRegion &R = regs[r];
+            while (!R.done) {
+                std::vector<double> need, needg, needa;
+                advance(R.fit, need, needg, needa);
+                if (R.fit.phase != Fit::DONE) {
+                    std::sort(need.begin(), need.end());
+                    need.erase(std::unique(need.begin(), need.end()), need.end());
+                    for (double x : need) {
+                        if (!(x > 0.0) || !std::isfinite(x)) {
+                            R.status = PCSF_EINVAL;
+                            R.done = true;
+                            break;
+                        }
+                        OmegaKey key = R.q;
+                        double rho = R.rho;
+                        if (R.stage == 0) rho = x;
+                        else key[0] = x;
+                        auto it = kidx.find(key);
+                        int m;
+                        if (it == kidx.end()) {
+                            m = (int)keys.size();
+                            kidx[key] = m;
+                            keys.push_back(key);
+                        } else {
+                            m = it->second;
+                        }
+                        Request q{};
+                        q.region = r;
+                        q.model = m;
+                        q.rho = rho;
+                        reqs.push_back(q);
+                        owner.push_back({r, x});
+                    }
+                    break;
+                }
+                // a fit finished: move along kr_map (OmegaModel.ml:171-190) and score (:195-219)
+                R.evals += (int)R.fit.cache.size();
+                if (R.fit.status != PCSF_OK) {
+                    R.status = R.fit.status;
+                    R.done = true;
+                    break;
+                }
+                if (R.stage == 0) {
+                    R.rho = R.fit.rho;
+                    R.stage = 1;
+                } else {
+                    R.q[0] = R.fit.rho;
+                    R.lpr_last = R.fit.lpr;
+                    R.stage = 0;
+                    R.round++;
+                }
+                if (R.round == 3) {
+                    if (R.hyp == 0) {
+                        R.lpr_h0 = R.lpr_last;
+                        R.rho_h0 = R.rho;
+                        R.kappa_h0 = R.q[0];
+                        R.hyp = 1;
+                        R.round = 0;
+                        R.q[1] = omega_h1;
+                        R.q[2] = sigma_h1;
+                    } else {
+                        R.done = true;
+                        break;
+                    }
+                }
+                R.start_fit();
+            }
+        }
+        if (reqs.empty()) break;
+        e->stats.rounds += 1;
+        int rc = dyn_prepare(e, dmod, keys, slot);
+        if (rc) return rc;
+        rc = evaluate(e, b, reqs, res, nullptr, true, &dmod.dm);
+        if (rc) return rc;
+        for (size_t k = 0; k < reqs.size(); k++) {
+            OmegaRegion &R = regs[owner[k].first];
+            Eval ev = res[k];
+            ev.lpr = prior_value(R.fit.prior_kind, owner[k].second) + ev.lpr;
+            R.fit.cache.push_back({owner[k].second, ev});
+        }
+    }
+    for (int r = 0; r < nreg; r++) {
+        const OmegaRegion &R = regs[r];
+        pcsf_omega_result &o = out[r];
+        std::memset(&o, 0, sizeof o);
+        o.status = R.status;
+        o.lpr_h0 = R.lpr_h0;
+        o.lpr_h1 = R.lpr_last;
+        o.rho_h0 = R.rho_h0;
+        o.kappa_h0 = R.kappa_h0;
+        o.rho_h1 = R.rho;
+        o.kappa_h1 = R.q[0];
+        o.score = 10.0 * (R.lpr_last - R.lpr_h0) / std::log(10.0);
+        o.evals = R.evals;
     }
     return PCSF_OK;
 }
@@ -1112,6 +1533,39 @@ int pcsf_engine_create_q(const pcsf_tree *tree, const double *Q_c, const double 
     return PCSF_OK;
 }
 
+int pcsf_engine_create_tree(const pcsf_tree *tree, int32_t flags, pcsf_engine **out)
+{
+    if (!out) {
+        g_static_error = "pcsf_engine_create_tree: out is NULL";
+        return PCSF_EINVAL;
+    }
+    *out = nullptr;
+    pcsf_engine *e = new (std::nothrow) pcsf_engine();
+    if (!e) {
+        g_static_error = "out of host memory";
+        return PCSF_ENOMEM;
+    }
+    int rc = engine_init_common(e, tree, flags);
+    if (rc != PCSF_OK) {
+        g_static_error = e->err;
+        delete e;
+        return rc;
+    }
+    *out = e;
+    return PCSF_OK;
+}
+
+int pcsf_omega_score(pcsf_engine *e, pcsf_batch *b, double omega_h1, double sigma_h1, pcsf_omega_result *out)
+{
+    if (!e) return PCSF_EINVAL;
+    CK(cudaSetDevice(e->device), "cudaSetDevice");
+    if (!b || b->e != e) return e->fail(PCSF_EINVAL, "pcsf_omega_score: batch does not belong to this engine");
+    if (b->nreg > 0 && !out) return e->fail(PCSF_EINVAL, "pcsf_omega_score: out is NULL");
+    if (!(omega_h1 >= 0.0) || !(sigma_h1 >= 0.0))
+        return e->fail(PCSF_EINVAL, "CamlPaml.P14n.instantiate_q: domain violation (omega_H1, sigma_H1 must be >= 0)");
+    return omega_impl(e, b, omega_h1, sigma_h1, out);
+}
+
 void pcsf_engine_destroy(pcsf_engine *e)
 {
     if (e) cudaSetDevice(e->device);
@@ -1152,6 +1606,7 @@ int pcsf_engine_eigensystem(const pcsf_engine *e, int32_t model, double *U, doub
 int pcsf_engine_pt(pcsf_engine *e, int32_t model, int32_t n_t, const double *t, double *P, int32_t *status)
 {
     if (!e) return PCSF_EINVAL;
+    if (!e->has_models) return e->fail(PCSF_EINVAL, "this engine has no coding / noncoding models");
     CK(cudaSetDevice(e->device), "cudaSetDevice");
     if (model < 0 || model > 1 || n_t <= 0 || !t || !P || !status) return e->fail(PCSF_EINVAL, "pcsf_engine_pt: bad argument");
     for (int i = 0; i < n_t; i++)
@@ -1253,6 +1708,7 @@ void pcsf_batch_destroy(pcsf_batch *b)
 int pcsf_score(pcsf_engine *e, pcsf_batch *b, int32_t strategy, pcsf_result *out)
 {
     if (!e) return PCSF_EINVAL;
+    if (!e->has_models) return e->fail(PCSF_EINVAL, "this engine has no coding / noncoding models");
     CK(cudaSetDevice(e->device), "cudaSetDevice");
     if (!b || b->e != e) return e->fail(PCSF_EINVAL, "pcsf_score: batch does not belong to this engine");
     if (b->nreg > 0 && !out) return e->fail(PCSF_EINVAL, "pcsf_score: out is NULL");
@@ -1274,6 +1730,7 @@ int pcsf_lpr(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, do
              int32_t *status)
 {
     if (!e) return PCSF_EINVAL;
+    if (!e->has_models) return e->fail(PCSF_EINVAL, "this engine has no coding / noncoding models");
     CK(cudaSetDevice(e->device), "cudaSetDevice");
     if (!b || b->e != e) return e->fail(PCSF_EINVAL, "pcsf_lpr: batch does not belong to this engine");
     if (model < 0 || model > 1) return e->fail(PCSF_EINVAL, "pcsf_lpr: model %d", model);
@@ -1284,7 +1741,7 @@ int pcsf_lpr(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, do
         reqs[r] = Request{r, model, 0, 0, rho[r]};
     }
     std::vector<Eval> res;
-    int rc = evaluate(e, b, reqs, res);
+    int rc = evaluate(e, b, reqs, res, nullptr, !e->tc_direct);
     if (rc) return rc;
     for (int r = 0; r < b->nreg; r++) {
         lpr[r] = res[r].lpr;
@@ -1298,6 +1755,7 @@ int pcsf_grad(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, d
               double *d_rho, int32_t *status)
 {
     if (!e) return PCSF_EINVAL;
+    if (!e->has_models) return e->fail(PCSF_EINVAL, "this engine has no coding / noncoding models");
     CK(cudaSetDevice(e->device), "cudaSetDevice");
     if (!b || b->e != e) return e->fail(PCSF_EINVAL, "pcsf_grad: batch does not belong to this engine");
     if (model < 0 || model > 1) return e->fail(PCSF_EINVAL, "pcsf_grad: model %d", model);

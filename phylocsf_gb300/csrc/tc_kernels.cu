@@ -13,14 +13,22 @@
 // identity part, v_c = alpha_c + D_c (E = P - I), so rounding in D only touches
 // the off-diagonal mass of P.
 //
-// Layout: 128 threads, thread t owns tile column (site) t, i.e. TMEM lane t.
+// Layout: 256 threads; thread t owns tile column (site) t % 128, i.e. TMEM lane
+// t % 128, and states 32*(t/128) .. +31 (warp w reaches lanes 32*(w%4)..).
 // TMEM (512 columns x 128 lanes x 32 bit): D_l cols [0,64), D_r [64,128), and
 // up to six parked partials alpha (64 columns each) from col 128.  Shared memory
 // holds the MMA operands in the K-major no-swizzle core-matrix layout (8 rows x
-// 16 bytes per core matrix): A (alpha, 128 x 64) hi/lo for two children and B
+// 16 bytes per core matrix), written with 16-byte stores so that a warp covers
+// one contiguous 512-byte run: A (alpha, 128 x 64) hi/lo for two children and B
 // (E row-major, 64 x 64) hi/lo for two children.  Leaf children are gathers of
-// E columns from the staged B operand.  Per-column rescaling by a power of two
-// is a per-thread operation here (one thread per site).
+// E^T rows from L2 while the MMAs run.  The per-column rescale exponent is the
+// maximum over the two threads of a column.
+//
+// Accuracy: the tensor cores' FP32 accumulation is not round-to-nearest (a
+// measured mean of -0.3 ulp per accumulation step of the 8-product chunks), so
+// these values carry a small systematic error.  The engine therefore uses this
+// kernel for the search evaluations of the rho maximisation and reports every
+// returned likelihood from the compensated FP32 kernel.
 //
 // Every mbarrier wait is bounded; on timeout the kernel records an error, waits
 // (again bounded) for its tensor-core work, releases its tensor memory and exits.
@@ -31,7 +39,7 @@
 
 namespace pcsf {
 
-constexpr int TCP_THREADS = 128;
+constexpr int TCP_THREADS = 256;     // two threads per tile column
 constexpr int TCP_M = 128;
 constexpr int TCP_MAX_SLOTS = 6;
 constexpr int TCP_MAX_LEAVES = 160;
@@ -114,10 +122,14 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_prune_tc(PruneArgs a, int *e
     __shared__ uint32_t tbase_s;
     __shared__ __align__(8) uint64_t bar;
     __shared__ SchedNode sched[TCP_MAX_LEAVES];
+    __shared__ float cmax[2][TCP_M];
+    __shared__ double zpart[2][2][TCP_M];
     __shared__ double red_l[TCP_THREADS / 32], red_e[TCP_THREADS / 32];
-    __shared__ int abort_s;
 
     const int tid = threadIdx.x, warp = tid >> 5;
+    const int site = tid & (TCP_M - 1);          // tile column = TMEM lane
+    const int half = tid >> 7;                    // states 32*half .. 32*half+31
+    const int s0 = 32 * half;
     const int nl = a.nl;
     uint8_t *lvT = sm + SM_LV;
     const uint32_t barA = smem_addr(&bar);
@@ -129,16 +141,13 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_prune_tc(PruneArgs a, int *e
                      :: "r"(smem_addr(&tbase_s)), "r"(TCP_TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(barA), "r"(1));
-        abort_s = 0;
-    }
+    if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(barA), "r"(1));
     for (int f = tid; f < a.n_internal; f += TCP_THREADS) sched[f] = a.sched[f];
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tbase = tbase_s;
-    const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+    const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;   // warp w reaches lanes 32*(w%4)..
     uint32_t phase = 0;
     bool ok = true;
 
@@ -154,42 +163,52 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_prune_tc(PruneArgs a, int *e
             int c = f / nl, l = f - c * nl;
             lvT[l * TCP_M + c] = (c < ncols) ? lg[f] : (uint8_t)K;
         }
-        int escale = 0;     // this thread's column: sum of rescale exponents
+        int escale = 0;     // this column's sum of rescale exponents
 
         for (int ni = 0; ni < a.n_internal && ok; ni++) {
             const SchedNode sn = sched[ni];
             const int slot_of[2] = {sn.lslot, sn.rslot};
             const int child[2] = {sn.lc, sn.rc};
-            // ---- stage B = E_c (row-major E[a][j]) hi / lo for both children
+            const bool any_mma = slot_of[0] >= 0 || slot_of[1] >= 0;
+            // ---- stage B = E_c (row-major E[a][j]) hi / lo for internal children; float4 per (a, 4 j)
 #pragma unroll
             for (int side = 0; side < 2; side++) {
+                if (slot_of[side] < 0) continue;
                 const float *g = Pbase + (size_t)child[side] * K2;   // E^T: g[j*64 + a] = E[a][j]
                 unsigned char *bh = sm + SM_B + side * 2 * B_BYTES;
                 unsigned char *bl = bh + B_BYTES;
-                for (int f = tid; f < K2; f += TCP_THREADS) {
-                    const int j = f >> 6, aa = f & 63;
-                    const float x = __ldg(g + f);
-                    const uint32_t o = core_off(aa, j, 8);
-                    *reinterpret_cast<float *>(bh + o) = x;
-                    *reinterpret_cast<float *>(bl + o) = x - tf32_hi(x);
+                for (int f = tid; f < 16 * K; f += TCP_THREADS) {
+                    const int aa = f & 63, q = f >> 6;
+                    float4 x;
+                    x.x = __ldg(g + (4 * q + 0) * K + aa);
+                    x.y = __ldg(g + (4 * q + 1) * K + aa);
+                    x.z = __ldg(g + (4 * q + 2) * K + aa);
+                    x.w = __ldg(g + (4 * q + 3) * K + aa);
+                    const float4 lo = make_float4(x.x - tf32_hi(x.x), x.y - tf32_hi(x.y), x.z - tf32_hi(x.z), x.w - tf32_hi(x.w));
+                    const uint32_t o = core_off(aa, 4 * q, 8);
+                    *reinterpret_cast<float4 *>(bh + o) = x;
+                    *reinterpret_cast<float4 *>(bl + o) = lo;
                 }
             }
-            // ---- stage A = alpha_c (site-major) hi / lo for internal children, from TMEM
+            // ---- stage A = alpha_c (site-major) hi / lo from TMEM; this thread's 32 states
 #pragma unroll
             for (int side = 0; side < 2; side++) {
                 if (slot_of[side] < 0) continue;
                 unsigned char *ah = sm + SM_A + side * 2 * A_BYTES;
                 unsigned char *al = ah + A_BYTES;
-                const uint32_t ts = tbase + lane_off + 128 + 64 * slot_of[side];
+                const uint32_t ts = tbase + lane_off + 128 + 64 * slot_of[side] + s0;
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
+                for (int q = 0; q < 2; q++) {
                     float x[16];
                     tmem_ld16(ts + 16 * q, x);
 #pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        const uint32_t o = core_off(tid, 16 * q + j, 16);
-                        *reinterpret_cast<float *>(ah + o) = x[j];
-                        *reinterpret_cast<float *>(al + o) = x[j] - tf32_hi(x[j]);
+                    for (int j4 = 0; j4 < 4; j4++) {
+                        const float4 hv = make_float4(x[4 * j4], x[4 * j4 + 1], x[4 * j4 + 2], x[4 * j4 + 3]);
+                        const float4 lv = make_float4(hv.x - tf32_hi(hv.x), hv.y - tf32_hi(hv.y), hv.z - tf32_hi(hv.z),
+                                                      hv.w - tf32_hi(hv.w));
+                        const uint32_t o = core_off(site, s0 + 16 * q + 4 * j4, 16);
+                        *reinterpret_cast<float4 *>(ah + o) = hv;
+                        *reinterpret_cast<float4 *>(al + o) = lv;
                     }
                 }
             }
@@ -197,7 +216,6 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_prune_tc(PruneArgs a, int *e
             tc_fence_before();
             __syncthreads();
             tc_fence_after();
-            const bool any_mma = slot_of[0] >= 0 || slot_of[1] >= 0;
             if (tid == 0 && any_mma) {
 #pragma unroll
                 for (int side = 0; side < 2; side++) {
@@ -221,63 +239,69 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_prune_tc(PruneArgs a, int *e
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                              :: "r"(barA) : "memory");
             }
+            // leaf children: gather E^T row s (L2) while the MMAs run
+            float v[32];
+#pragma unroll
+            for (int side = 0; side < 2; side++) {
+                if (slot_of[side] >= 0) continue;
+                const int s = lvT[child[side] * TCP_M + site];
+                const float4 *row = reinterpret_cast<const float4 *>(Pbase + (size_t)child[side] * K2 + (size_t)(s < K ? s : 0) * K + s0);
+#pragma unroll
+                for (int j4 = 0; j4 < 8; j4++) {
+                    float4 x = make_float4(1.f, 1.f, 1.f, 1.f);
+                    if (s < K) {
+                        x = __ldg(row + j4);
+                        const int a0 = s0 + 4 * j4;
+                        if (s >= a0 && s < a0 + 4) (&x.x)[s - a0] += 1.0f;
+                    }
+                    const float u[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+                    for (int k = 0; k < 4; k++) v[4 * j4 + k] = (side && slot_of[0] < 0) ? v[4 * j4 + k] * u[k] : u[k];
+                }
+            }
             if (any_mma) {
                 bool done = mbar_wait(barA, phase);
                 phase ^= 1u;
                 if (__syncthreads_or(!done)) {
-                    if (tid == 0) {
-                        atomicExch(err, 1);
-                        abort_s = 1;
-                    }
-                    mbar_wait(barA, phase ^ 1u);   // give the in-flight MMAs a second bounded wait
+                    if (tid == 0) atomicExch(err, 1);
+                    mbar_wait(barA, phase ^ 1u);   // a second bounded wait for the in-flight MMAs
                     ok = false;
                     break;
                 }
             }
             tc_fence_after();
-            // ---- epilogue: v_l * v_r for this thread's column, rescale, park in TMEM
-            float v[64];
+            // ---- epilogue: internal children v = alpha + D, product with the other child
 #pragma unroll
             for (int side = 0; side < 2; side++) {
-                const unsigned char *bh = sm + SM_B + side * 2 * B_BYTES;
-                const unsigned char *bl = bh + B_BYTES;
-                if (slot_of[side] >= 0) {
-                    const uint32_t tD = tbase + lane_off + 64 * side;
-                    const uint32_t tS = tbase + lane_off + 128 + 64 * slot_of[side];
+                if (slot_of[side] < 0) continue;
+                const uint32_t tD = tbase + lane_off + 64 * side + s0;
+                const uint32_t tS = tbase + lane_off + 128 + 64 * slot_of[side] + s0;
+                // does v already hold the other child's partial?
+                const bool have_other = (side == 1) || (slot_of[1] < 0);
 #pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        float d[16], x[16];
-                        tmem_ld16(tD + 16 * q, d);
-                        tmem_ld16(tS + 16 * q, x);
+                for (int q = 0; q < 2; q++) {
+                    float d[16], x[16];
+                    tmem_ld16(tD + 16 * q, d);
+                    tmem_ld16(tS + 16 * q, x);
 #pragma unroll
-                        for (int j = 0; j < 16; j++) {
-                            const float u = x[j] + d[j];
-                            v[16 * q + j] = side ? v[16 * q + j] * u : u;
-                        }
-                    }
-                } else {
-                    const int s = lvT[child[side] * TCP_M + tid];
-#pragma unroll
-                    for (int aa = 0; aa < 64; aa++) {
-                        float u = 1.0f;
-                        if (s < K) {
-                            const uint32_t o = core_off(aa, s, 8);
-                            u = *reinterpret_cast<const float *>(bh + o) + *reinterpret_cast<const float *>(bl + o);
-                            if (aa == s) u += 1.0f;
-                        }
-                        v[aa] = side ? v[aa] * u : u;
+                    for (int j = 0; j < 16; j++) {
+                        const float u = x[j] + d[j];
+                        v[16 * q + j] = have_other ? v[16 * q + j] * u : u;
                     }
                 }
             }
             float mx = 0.0f;
 #pragma unroll
-            for (int aa = 0; aa < 64; aa++) mx = fmaxf(mx, v[aa]);
+            for (int k = 0; k < 32; k++) mx = fmaxf(mx, v[k]);
+            cmax[half][site] = mx;
+            __syncthreads();
+            mx = fmaxf(cmax[0][site], cmax[1][site]);
             int e = 0;
             if (mx > 0.0f) frexpf(mx, &e);
             escale += e;
-            const uint32_t tO = tbase + lane_off + 128 + 64 * sn.oslot;
+            const uint32_t tO = tbase + lane_off + 128 + 64 * sn.oslot + s0;
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
+            for (int q = 0; q < 2; q++) {
                 float y[16];
 #pragma unroll
                 for (int j = 0; j < 16; j++) y[j] = ldexpf(v[16 * q + j], -e);
@@ -290,14 +314,13 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_prune_tc(PruneArgs a, int *e
         }
         if (!ok) break;
         // ---- root: z = alpha_root . prior, elpr term, FP64 sums over the tile
-        double tl = 0.0, te = 0.0;
         {
-            const uint32_t tR = tbase + lane_off + 128 + 64 * sched[a.n_internal - 1].oslot;
-            const double *pr = a.m.prior + md * K;
-            const double *wl = a.m.wlog + md * K;
+            const uint32_t tR = tbase + lane_off + 128 + 64 * sched[a.n_internal - 1].oslot + s0;
+            const double *pr = a.m.prior + md * K + s0;
+            const double *wl = a.m.wlog + md * K + s0;
             double z = 0.0, wz = 0.0;
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
+            for (int q = 0; q < 2; q++) {
                 float x[16];
                 tmem_ld16(tR + 16 * q, x);
 #pragma unroll
@@ -306,13 +329,19 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_prune_tc(PruneArgs a, int *e
                     wz += (double)x[j] * wl[16 * q + j];
                 }
             }
-            if (tid < ncols) {
-                if (z > 0.0) {
-                    tl = log(z) + (double)escale * 0.69314718055994530942;
-                    te = wz / z;
-                } else {
-                    tl = -INFINITY;
-                }
+            zpart[half][0][site] = z;
+            zpart[half][1][site] = wz;
+        }
+        __syncthreads();
+        double tl = 0.0, te = 0.0;
+        if (half == 0 && site < ncols) {
+            const double z = zpart[0][0][site] + zpart[1][0][site];
+            const double wz = zpart[0][1][site] + zpart[1][1][site];
+            if (z > 0.0) {
+                tl = log(z) + (double)escale * 0.69314718055994530942;
+                te = wz / z;
+            } else {
+                tl = -INFINITY;
             }
         }
 #pragma unroll

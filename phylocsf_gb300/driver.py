@@ -78,6 +78,35 @@ def translate(dna: str) -> str:
     return "".join(out)
 
 
+def bls(tree: E.Tree, aln: List[str], leaf_rows: List[Optional[int]], lo: int, hi: int) -> float:
+    """Branch length score of nucleotide columns lo..hi (src/PhyloCSF.ml:252-262).
+
+    Per column, the reference takes Newick.subtree over the species present in
+    that column (not '-', '.', 'N') and its total length without the root branch
+    (Newick.ml:34-61): the length of the smallest subtree spanning those species.
+    An edge above node v belongs to it exactly when some but not all of the
+    present species lie below v.  The sum over columns is divided by the full
+    tree's length times the column count.
+    """
+    n, nl = tree.n, tree.nl
+    ncol = hi - lo + 1
+    pres = np.zeros((ncol, nl), np.int32)
+    for l in range(nl):
+        r = leaf_rows[l]
+        if r is None:
+            continue
+        row = np.frombuffer(aln[r][lo:hi + 1].encode(), np.uint8)
+        pres[:, l] = ~np.isin(row, np.frombuffer(b"-.N", np.uint8))
+    below = np.zeros((ncol, n), np.int32)
+    below[:, :nl] = pres
+    for i in range(n - 1):                      # children precede parents in T order
+        below[:, tree.parent[i]] += below[:, i]
+    total = below[:, n - 1:n]
+    inside = (below[:, : n - 1] > 0) & (below[:, : n - 1] < total)
+    bl_total = float((inside * tree.branch[None, : n - 1]).sum())
+    return bl_total / (float(tree.branch[: n - 1].sum()) * ncol)
+
+
 @dataclass
 class Options:
     strategy: int = E.MLE
@@ -90,6 +119,7 @@ class Options:
     all_scores: bool = False
     dna: bool = False
     aa: bool = False
+    bls: bool = False
 
 
 @dataclass
@@ -148,6 +178,8 @@ def process_alignment(engine: E.Engine, text: str, opts: Options, fn: str = "") 
             s += "\t%d\t%d" % (rs.lo, rs.hi)
         if six:
             s += "\t" + ("-" if rs.rc else "+")
+        if opts.bls:
+            s += "\t%.4f" % bls(tree, rc_aln if rs.rc else aln, leaf_rows, rs.lo, rs.hi)
         if opts.anc_comp:
             s += "\t%.4f" % rs.result["anc_comp_score"]
         refdna = (rc_aln if rs.rc else aln)[0][rs.lo:rs.hi + 1]

@@ -27,7 +27,8 @@ STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memo
                 10: "capacity exceeded"}
 FIXED, MLE = 0, 1
 PREC = {"fp64": 0, "fp32": 1, "tf32x3": 2, "bf16x3": 3, "tf32": 4,
-        "fp32c": 1 | (1 << 16)}     # fp32c: FP32 contractions with compensated summation
+        "fp32c": 1 | (1 << 16),      # FP32 contractions with compensated summation
+        "tf32x3_direct": 2 | (1 << 17), "tf32_direct": 4 | (1 << 17)}   # lpr straight from the tensor cores
 MARGINALIZE = 64
 ORF_MODES = {"asis": 0, "atgstop": 1, "stopstop": 2, "stopstop3": 3, "tofirststop": 4,
              "fromlaststop": 5, "toorfromstop": 6}
@@ -58,6 +59,17 @@ RESULT_DTYPE = np.dtype([("score", "f8"), ("anc_comp_score", "f8"), ("rho_c", "f
 assert RESULT_DTYPE.itemsize == ctypes.sizeof(Result)
 
 
+class OmegaResult(ctypes.Structure):
+    _fields_ = [("score", ctypes.c_double), ("lpr_h0", ctypes.c_double), ("lpr_h1", ctypes.c_double),
+                ("rho_h0", ctypes.c_double), ("kappa_h0", ctypes.c_double), ("rho_h1", ctypes.c_double),
+                ("kappa_h1", ctypes.c_double), ("status", ctypes.c_int32), ("evals", ctypes.c_int32)]
+
+
+OMEGA_DTYPE = np.dtype([("score", "f8"), ("lpr_h0", "f8"), ("lpr_h1", "f8"), ("rho_h0", "f8"), ("kappa_h0", "f8"),
+                        ("rho_h1", "f8"), ("kappa_h1", "f8"), ("status", "i4"), ("evals", "i4")])
+assert OMEGA_DTYPE.itemsize == ctypes.sizeof(OmegaResult)
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("kernel_launches", ctypes.c_int64), ("evaluations", ctypes.c_int64),
                 ("column_branches", ctypes.c_int64), ("rounds", ctypes.c_int64),
@@ -75,6 +87,8 @@ SIGNATURES = {
     "pcsf_engine_create": ([ctypes.POINTER(_Tree), _D, _D, _D, _D, ctypes.c_int32, ctypes.POINTER(_VP)], ctypes.c_int),
     "pcsf_engine_create_q": ([ctypes.POINTER(_Tree), _D, _D, _D, _D, _D, _D, ctypes.c_int32, ctypes.POINTER(_VP)],
                              ctypes.c_int),
+    "pcsf_engine_create_tree": ([ctypes.POINTER(_Tree), ctypes.c_int32, ctypes.POINTER(_VP)], ctypes.c_int),
+    "pcsf_omega_score": ([_VP, _VP, ctypes.c_double, ctypes.c_double, ctypes.POINTER(OmegaResult)], ctypes.c_int),
     "pcsf_engine_destroy": ([_VP], None),
     "pcsf_last_error": ([_VP], ctypes.c_char_p),
     "pcsf_engine_get_stats": ([_VP, ctypes.POINTER(Stats)], ctypes.c_int),
@@ -278,7 +292,9 @@ class Engine:
         flags = PREC[precision] | (0 if device is None else (device + 1) << 8)
         ct, keep = tree.c_struct()
         h = _VP()
-        if Q is None:
+        if Q == "tree":
+            rc = self.lib.pcsf_engine_create_tree(ctypes.byref(ct), flags, ctypes.byref(h))
+        elif Q is None:
             arrs = [np.ascontiguousarray(x, np.float64) for x in (S_c, pi_c, S_n, pi_n)]
             rc = self.lib.pcsf_engine_create(ctypes.byref(ct), *[_p(a, ctypes.c_double) for a in arrs], flags,
                                              ctypes.byref(h))
@@ -293,6 +309,18 @@ class Engine:
     def from_q(cls, tree: Tree, Q_c, eq_c, prior_c, Q_n, eq_n, prior_n, precision: str = "fp32",
                device: Optional[int] = None) -> "Engine":
         return cls(tree, precision=precision, Q=(Q_c, eq_c, prior_c, Q_n, eq_n, prior_n), device=device)
+
+    @classmethod
+    def for_tree(cls, tree: Tree, precision: str = "fp64", device: Optional[int] = None) -> "Engine":
+        """An engine without fixed models, for the OmegaModel test."""
+        return cls(tree, precision=precision, Q="tree", device=device)
+
+    def omega_score(self, batch: Batch, omega_h1: float = 0.2, sigma_h1: float = 0.01) -> np.ndarray:
+        """OmegaModel.score (src/OmegaModel.ml:195-219) for every region of the batch."""
+        out = np.zeros(batch.n_regions, OMEGA_DTYPE)
+        _check(self.lib.pcsf_omega_score(self.handle, batch.handle, omega_h1, sigma_h1,
+                                         out.ctypes.data_as(ctypes.POINTER(OmegaResult))), self.handle)
+        return out
 
     def close(self):
         if getattr(self, "handle", None):

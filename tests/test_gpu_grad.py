@@ -1,7 +1,9 @@
 """GPU adjoint gradient (pcsf_grad) against the oracle's outside pass and finite differences.
 
-Tolerances: FP64 engine, per-branch d lpr / d t within 1e-8 relative (abs
-floor 1e-8) of the oracle; FP32 (compensated) within 1e-3 relative of the
+Tolerances: FP64 engine, per-branch d lpr / d t within 1e-7 relative (abs
+floor 1e-8) of the oracle (the oracle differentiates P(t) = exp(tQ)
+analytically, the kernel applies dP/dt = Q P to P after the clamp /
+renormalise row rule); FP32 (compensated) within 1e-3 relative of the
 largest |gradient| entry.  d lpr / d rho against a central difference of the
 FP64 engine's lpr with h = 1e-5: within 1e-6 relative.
 """
@@ -56,7 +58,9 @@ def test_branch_gradient_matches_oracle(prec, name):
                     continue
                 if prec == "fp64":
                     assert lpr[r] == pytest.approx(lo, rel=1e-9)
-                    assert np.allclose(db[r], go, rtol=1e-8, atol=1e-8)
+                    err = np.abs(db[r] - go) - (1e-7 * np.abs(go) + 1e-8)
+                    k = int(np.argmax(err))
+                    assert err[k] <= 0, (model, rho, r, k, db[r][k], go[k], tree.branch[k])
                 else:
                     scale = np.abs(go).max()
                     assert np.abs(db[r] - go).max() <= 1e-3 * scale + 1e-6, (np.abs(db[r] - go).max(), scale)

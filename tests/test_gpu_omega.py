@@ -1,0 +1,62 @@
+"""OmegaModel test on the GPU (pcsf_omega_score) against the oracle restatement (oracle/omega.py).
+
+Tolerances: FP64 engine |d score| <= 1e-6 dB and kappa / rho within 1e-7
+relative (same iterates as the oracle); compensated-FP32 engine |d score| <=
+1e-2 dB (its P(t) is formed in FP64; the pruning is FP32 and the coordinate
+ascent may take different Brent steps).
+"""
+import numpy as np
+import pytest
+
+import phylocsf_gb300 as P
+from phylocsf_gb300 import synth
+from oracle import oracle as O
+from oracle import omega as W
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _fast():
+    O.set_sparse_leaves(True)
+
+
+def _regions(name, lengths, seed):
+    ps = synth.load_params(name)
+    rng = np.random.default_rng(seed)
+    gf = synth.gap_fractions(rng, len(lengths), ps.tree.nl, 0.05, 0.3, 0.1)
+    return ps, *synth.simulate(ps, np.asarray(lengths), (np.arange(len(lengths)) % 2).astype(np.int32), gf, seed)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+def test_omega_matches_oracle(prec):
+    ps, offs, leaves = _regions("12flies", [30, 45, 0], seed=13)
+    tree, *_ = H.fixture_params("12flies")
+    e = P.Engine.for_tree(ps.tree, precision=prec)
+    res = e.omega_score(e.batch(offs, leaves), 0.2, 0.01)
+    for r in range(len(offs) - 1):
+        lv = H.u8_to_oracle(leaves[offs[r]:offs[r + 1]])
+        sc, l0, l1, q0, r0, q1, r1, _ = W.score(tree, lv)
+        g = res[r]
+        assert g["status"] == 0
+        if prec == "fp64":
+            assert abs(g["score"] - sc) <= 1e-6, (r, g["score"], sc)
+            assert g["kappa_h0"] == pytest.approx(q0[0], rel=1e-7)
+            assert g["rho_h0"] == pytest.approx(r0, rel=1e-7)
+            assert g["kappa_h1"] == pytest.approx(q1[0], rel=1e-7)
+            assert g["rho_h1"] == pytest.approx(r1, rel=1e-7)
+        else:
+            assert abs(g["score"] - sc) <= 1e-2, (r, g["score"], sc)
+
+
+def test_omega_reference_example():
+    """The tal-AA example on 12flies: the GPU and the oracle agree on the omega test."""
+    tree, *_ = H.fixture_params("12flies")
+    ps = synth.load_params("12flies")
+    ex = H.examples()["tal-AA.fa"]
+    lv = O.pleaves(ex["rows"], O.leaf_rows_for(tree, ex["species"]), 0, len(ex["rows"][0]) - 1)
+    e = P.Engine.for_tree(ps.tree, precision="fp64")
+    g = e.omega_score(e.batch(np.array([0, lv.shape[0]], np.int64), H.oracle_leaves_to_u8(lv)))[0]
+    sc = W.score(tree, lv)[0]
+    assert g["status"] == 0 and abs(g["score"] - sc) <= 1e-6
