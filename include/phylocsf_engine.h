@@ -189,6 +189,29 @@ int pcsf_lpr(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, do
 int pcsf_grad(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, double *lpr, double *d_branch,
               double *d_rho, int32_t *status);
 
+/* ------------------------------------------------------- allocation-free */
+
+/* Size of the fixed device scratch area behind pcsf_lpr_noalloc. */
+#define PCSF_NOALLOC_SCRATCH_BYTES (24u << 20)
+
+/* lpr and elpr of every region under model m at one tree scale rho, without
+ * allocating anything.  No counterpart in the reference: it exists for callers
+ * that cannot call cudaMalloc when they need a likelihood (a host framework
+ * that owns all device memory through its own pool, a latency-critical thread
+ * that cannot take cudaMalloc's implicit synchronisation, a process at a hard
+ * device-memory cap).  d_leaves ([total_cols][n_leaves], codes as in
+ * pcsf_batch_create), d_lpr and d_elpr ([n_regions]; d_elpr may be NULL) are
+ * DEVICE pointers owned by the caller; col_offsets is a host array.  Scratch
+ * comes from one PCSF_NOALLOC_SCRATCH_BYTES array compiled into the library
+ * (held by every GPU that loads it until exit); a batch that does not fit
+ * (more than 32768 regions, more than 131072 column tiles, or more than the
+ * area) fails with PCSF_ERANGE.  The first call on a device looks up the
+ * array's device address, so make it before any stream capture.  Calls share
+ * the area: calls that overlap on the GPU, or run concurrently from several
+ * host threads, race.  Returns after the results are written. */
+int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32_t n_regions, const int64_t *col_offsets,
+                     const uint8_t *d_leaves, double *d_lpr, double *d_elpr);
+
 /* ------------------------------------------------------------ OmegaModel */
 
 /* One region's dN/dS test (OmegaModel.score, src/OmegaModel.ml:195-219). */

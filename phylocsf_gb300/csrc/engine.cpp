@@ -1111,6 +1111,33 @@ static int score_impl(pcsf_engine *e, pcsf_batch *b, int strategy, pcsf_result *
 }
 
 // ---------------------------------------------------------------------------
+// Read-only view of an engine's device state for pcsf_lpr_noalloc (noalloc.cu).
+
+int pcsf_internal_noalloc_ctx(pcsf_engine *e, int *device, cudaStream_t *stream, int *prec, int *compensated, int *nl,
+                              int *nbr, const double **branch, const SchedNode **sched, int *n_internal, int *nslots,
+                              DevModels *m, int *sm_count, int *prune_grid, int **derr)
+{
+    *device = e->device;
+    *stream = e->stream;
+    *prec = e->prec;
+    *compensated = e->compensated ? 1 : 0;
+    *nl = e->nl;
+    *nbr = e->nbr;
+    *branch = e->dbranch.p;
+    *sched = e->dsched.p;
+    *n_internal = (int)e->sched.size();
+    *nslots = e->nslots;
+    *m = e->dm;
+    *sm_count = e->sm_count;
+    *prune_grid = e->prune_grid;
+    *derr = e->derr.p;
+    return PCSF_OK;
+}
+
+int pcsf_internal_fail(pcsf_engine *e, int code, const char *msg) { return e->fail(code, "%s", msg); }
+
+
+// ---------------------------------------------------------------------------
 // OmegaModel (src/OmegaModel.ml): parametric codon Q, priors, and the H0/H1
 // maximum-a-posteriori fits of rho and kappa.
 
