@@ -37,6 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "codon-column·branches/s and regions scored/s at |Δscore|≤1e-3 dB vs FP64 oracle"
+L2_BYTES = 129 * 1024 * 1024
 
 
 def flops_per_column(nl: int) -> int:
@@ -233,8 +234,19 @@ def run_ours(args, world, rank, local):
     stream = torch.cuda.ExternalStream(eng.stream_handle(), device=torch.device("cuda", local))
     batch = eng.batch(wl.col_offsets, wl.leaves)
 
+    # inputs smaller than twice the L2 (129 MB) get an L2 flush before every timed step
+    flush = None
+    if wl.leaves.nbytes < 2 * L2_BYTES:
+        flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=torch.device("cuda", local))
+
+    def step():
+        if flush is not None:
+            with torch.cuda.stream(stream):
+                flush.fill_(0.0)
+        return eng.score(batch, wl.strategy)
+
     for _ in range(args.warmup):
-        res = eng.score(batch, wl.strategy)
+        res = step()
     clocks = ClockSampler(local) if rank == 0 else None
     eng.reset_stats()
     barrier(world)
@@ -243,7 +255,7 @@ def run_ours(args, world, rank, local):
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     for _ in range(args.steps):
-        res = eng.score(batch, wl.strategy)
+        res = step()
     ev1.record(stream)
     ev1.synchronize()
     torch.cuda.synchronize(local)
@@ -265,6 +277,9 @@ def run_ours(args, world, rank, local):
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
+        if flush is not None:
+            with torch.cuda.stream(stream):
+                flush.fill_(0.0)
         res_e2e = eng.score_batch(offs_pinned, leaves_pinned, wl.strategy)
     e1.record(stream)
     e1.synchronize()
@@ -293,7 +308,8 @@ def run_ours(args, world, rank, local):
             "data": "synthetic (seeded simulation along the tree; no public benchmark exists)",
             "config": {"workload": wl.name, "tree": ps.name, "strategy": "mle" if wl.strategy else "fixed",
                        "regions_per_gpu": wl.n_regions, "columns_per_gpu": wl.total_cols,
-                       "precision": args.precision, "l2": "inputs larger than L2 (%.0f MB)" % (wl.leaves.nbytes / 1e6),
+                       "precision": args.precision, "l2": ("L2 flushed before every timed step (inputs %.0f MB)" if flush is not None
+                              else "inputs larger than L2 (%.0f MB)") % (wl.leaves.nbytes / 1e6),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "column_branches_per_s": colb_per_s,
             "e2e": {"value": e2e_value, "unit": "regions/s", "h2d_bytes_per_step": int(wl.leaves.nbytes +

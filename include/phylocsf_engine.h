@@ -58,6 +58,11 @@ extern "C" {
  * accumulation of many small positive terms into a large sum drops the ones
  * below half an ulp, a bias that accumulates over thousands of columns. */
 #define PCSF_COMPENSATED (1 << 16)
+/* engine flag: blocked compensation -- eight products summed plainly, each block
+ * folded in with Kahan's correction (about a ninth of the plain bias, a third of
+ * the cost of PCSF_COMPENSATED).  Also selects the kernel that produces the
+ * returned values of the tensor-core modes. */
+#define PCSF_BLOCK_COMPENSATED (1 << 18)
 
 /* engine flag for the tensor-core modes: pcsf_lpr returns the tensor-core
  * kernel's values instead of the compensated FP32 kernel's (precision study). */

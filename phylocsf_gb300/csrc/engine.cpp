@@ -101,7 +101,10 @@ struct pcsf_engine {
     cudaEvent_t ev[8] = {};
     int prec = PCSF_PREC_FP32;
     bool compensated = false;
+    bool block_comp = false;
     bool tc_direct = false;
+    int comp_mode() const { return compensated ? 1 : block_comp ? 2 : 0; }
+    int accurate_comp() const { return block_comp ? 2 : 1; }
     bool has_models = false;
     std::string err;
 
@@ -294,13 +297,16 @@ static int assemble_q(const double *S, const double *pi, double *Q)
 }
 
 // FP32 P(t) formation support: E(t_g) = P(t_g) - I on a geometric grid
-// t_g = t0 r^g (t0 = 1e-5, r = 1.01) formed in FP64 and stored in FP32, plus
+// t_g = t0 r^g (t0 = 1e-5, r = 1.002) formed in FP64 and stored in FP32, plus
 // Q and Q^2 for t < t0.  A branch then needs only the FP32 correction
 // D^-1/2 U diag(e^{lam t} - e^{lam t_g}) U^T D^1/2, whose rounding error is
-// proportional to |t - t_g| <= 0.5% of t instead of t itself.
+// proportional to |t - t_g| <= 0.1% of t instead of t itself.  (The eigen-sum
+// cancels heavily on the small entries of E; with r = 1.01 the correction's
+// rounding still cost ~8e-5 nats per 3000 codons at rho = 0.05.)  About 6,200
+// grid points per model for the bundled trees: 0.2 GB of FP32 matrices.
 static int build_pt_grid(pcsf_engine *e, const double *Q[2])
 {
-    const double t0 = 1e-5, ratio = 1.01;
+    const double t0 = 1e-5, ratio = 1.002;
     double bmax = 0.0;
     for (double b : e->branch) bmax = std::max(bmax, b);
     const double tmax = std::max(10.5 * bmax, 1.0);
@@ -455,6 +461,7 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
         return e->fail(PCSF_EINVAL, "precision mode %d is not available in this build", prec);
     e->prec = prec;
     e->compensated = (flags & PCSF_COMPENSATED) != 0;
+    e->block_comp = (flags & PCSF_BLOCK_COMPENSATED) != 0;
     e->tc_direct = (flags & PCSF_TC_DIRECT) != 0;
     int ndev = 0;
     cudaError_t ce = cudaGetDeviceCount(&ndev);
@@ -534,7 +541,8 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     const bool tc = (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32) && !accurate;
     // the gradient always runs the SIMT adjoint kernel (64-column tiles in FP32)
     const int TC = (grad || !tc) ? (e->prec == PCSF_PREC_FP64 ? 32 : 64) : prune_tile_cols(e->prec);
-    const bool simt_comp = e->compensated || accurate;
+    const int comp = (accurate && (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32)) ? e->accurate_comp()
+                                                                                              : e->comp_mode();
 
     // work items, P-set dedup and chunking (at most pbuf_psets distinct P sets per chunk)
     std::vector<Request> reqs(reqs_in);
@@ -634,7 +642,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         if (stage64) {
             CK(launch_pform(true, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, dmv, e->Pbuf64.p, e->dstatus.p + p0, s),
                "P(t) formation launch");
-            CK(launch_d2f(e->Pbuf64.p, reinterpret_cast<float *>(e->Pbuf.p), (size_t)(p1 - p0) * e->nbr * K2, s),
+            CK(launch_d2f_rows(e->Pbuf64.p, reinterpret_cast<float *>(e->Pbuf.p), (size_t)(p1 - p0) * e->nbr, s),
                "P(t) conversion launch");
             e->stats.kernel_launches += 1;
         } else {
@@ -674,14 +682,15 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
             ga.partials = pa.partials;
             ga.gpart = e->dgpart.p + (size_t)wib[r0] * e->nbr;
             int grid = std::min(e->grad_grid, std::max(pa.nwi, 1));
+            const bool tce = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
             CK(launch_grad(e->prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32,
-                           e->compensated || tc, ga, s, grid), "gradient launch");
+                           tce ? e->accurate_comp() : e->comp_mode(), ga, s, grid), "gradient launch");
         } else if (tc) {
             int grid = std::min(e->sm_count, std::max(pa.nwi, 1));
             CK(launch_prune_tc(e->prec == PCSF_PREC_TF32X3 ? 3 : 1, pa, e->derr.p, s, grid), "tensor-core pruning launch");
         } else {
             int grid = std::min(e->prune_grid, std::max(pa.nwi, 1));
-            CK(launch_prune(e->prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32, simt_comp, pa, s, grid),
+            CK(launch_prune(e->prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32, comp, pa, s, grid),
                "pruning launch");
         }
         CK(cudaEventRecord(e->ev[2], s), "event");
@@ -1120,7 +1129,7 @@ int pcsf_internal_noalloc_ctx(pcsf_engine *e, int *device, cudaStream_t *stream,
     *device = e->device;
     *stream = e->stream;
     *prec = e->prec;
-    *compensated = e->compensated ? 1 : 0;
+    *compensated = e->comp_mode();
     *nl = e->nl;
     *nbr = e->nbr;
     *branch = e->dbranch.p;

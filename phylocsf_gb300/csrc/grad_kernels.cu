@@ -47,7 +47,7 @@ struct GradLayout {
     }
 };
 
-template <typename T, int TC, bool KAHAN>
+template <typename T, int TC, int KAHAN>
 __global__ void __launch_bounds__(GR_THREADS) k_grad(GradArgs a)
 {
     constexpr int CPT = TC / 16;
@@ -291,7 +291,7 @@ size_t grad_smem_bytes(int prec, int nslots, int nl, int nint)
     return GradLayout<float, 64>::smem(nslots, nl, nint);
 }
 
-template <typename T, int TC, bool KAHAN>
+template <typename T, int TC, int KAHAN>
 static cudaError_t launch_grad_t(const GradArgs &a, cudaStream_t s, int grid)
 {
     size_t smem = GradLayout<T, TC>::smem(a.nslots, a.nl, a.n_internal);
@@ -301,12 +301,13 @@ static cudaError_t launch_grad_t(const GradArgs &a, cudaStream_t s, int grid)
     return cudaGetLastError();
 }
 
-cudaError_t launch_grad(int prec, bool compensated, const GradArgs &a, cudaStream_t s, int grid)
+cudaError_t launch_grad(int prec, int comp, const GradArgs &a, cudaStream_t s, int grid)
 {
     if (a.nwi <= 0) return cudaSuccess;
-    if (prec == PCSF_PREC_FP64) return launch_grad_t<double, 32, false>(a, s, grid);
-    if (compensated) return launch_grad_t<float, 64, true>(a, s, grid);
-    return launch_grad_t<float, 64, false>(a, s, grid);
+    if (prec == PCSF_PREC_FP64) return launch_grad_t<double, 32, 0>(a, s, grid);
+    if (comp == 1) return launch_grad_t<float, 64, 1>(a, s, grid);
+    if (comp == 2) return launch_grad_t<float, 64, 2>(a, s, grid);
+    return launch_grad_t<float, 64, 0>(a, s, grid);
 }
 
 // grad[r][c] = sum of gpart over request r's work items (fixed order)

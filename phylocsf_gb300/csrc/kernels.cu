@@ -279,8 +279,12 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
                 if (w != 0.0) rs += U[i * K + mm] * ex[mm] * w;
             }
             rs *= isq[i];
+            // the diagonal is the FP64 sum of the stored (rounded) off-diagonal
+            // entries, so every stored row of P = I + E sums to 1 to within one
+            // rounding of the diagonal; a plain FP32 sum here biases lpr by
+            // ~1e-4 nats per 3000 codons at rho = 1
             bool neg = false;
-            T diag = (T)0;
+            double diag = 0.0;
             for (int j = 0; j < K; j++) {
                 T x = Es[i * (K + 1) + j];
                 if (j == i) {
@@ -292,12 +296,12 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
                     x = (T)0;
                     Es[i * (K + 1) + j] = x;
                 }
-                diag -= x;
+                diag -= (double)x;
             }
             if (neg) status_min(status_key + r, b, i, PCSF_ENEGP);
             else if (fabs(rs) > m.tol) status_min(status_key + r, b, i, PCSF_EROWSUM);
-            else if (!((double)diag > -1.0)) status_min(status_key + r, b, i, PCSF_EDIAG);
-            Es[i * (K + 1) + i] = diag;
+            else if (!(diag > -1.0)) status_min(status_key + r, b, i, PCSF_EDIAG);
+            Es[i * (K + 1) + i] = (T)diag;
         }
         __syncthreads();
         T *out = Pbuf + ((size_t)r * nbr + b) * K2;
@@ -341,6 +345,33 @@ cudaError_t launch_d2f(const double *in, float *out, size_t n, cudaStream_t s)
     return cudaGetLastError();
 }
 
+// FP64 -> FP32 for E^T matrices that already obey the row rule: off-diagonal
+// entries are rounded and each diagonal is re-formed as the FP64 sum of its
+// row's rounded entries (storage E^T: element (i, j) of E at [j*K + i]).
+__global__ void __launch_bounds__(256) k_d2f_rows(const double *in, float *out, size_t nmat)
+{
+    const size_t mat = blockIdx.x * (size_t)4 + threadIdx.x / K;
+    const int i = threadIdx.x % K;
+    if (mat >= nmat) return;
+    const double *src = in + mat * K2;
+    float *dst = out + mat * K2;
+    double d = 0.0;
+    for (int j = 0; j < K; j++) {
+        if (j == i) continue;
+        const float x = (float)src[j * K + i];
+        dst[j * K + i] = x;
+        d -= (double)x;
+    }
+    dst[i * K + i] = (float)d;
+}
+
+cudaError_t launch_d2f_rows(const double *in, float *out, size_t nmat, cudaStream_t s)
+{
+    if (nmat == 0) return cudaSuccess;
+    k_d2f_rows<<<(unsigned)((nmat + 3) / 4), 256, 0, s>>>(in, out, nmat);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // Pruning (inside pass).  One CTA (256 threads) owns a tile of TC columns of
 // one request's region and walks the internal nodes in the register-minimal
@@ -373,7 +404,7 @@ struct PruneSmem {
     }
 };
 
-template <typename T, int TC, bool KAHAN>
+template <typename T, int TC, int KAHAN>
 __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
 {
     constexpr int CPT = TC / 16;
@@ -501,7 +532,7 @@ size_t prune_smem_bytes(int prec, int nslots, int nl, int nint)
     return PruneSmem<float, 64>::bytes(nslots, nl, nint);
 }
 
-template <typename T, int TC, bool KAHAN>
+template <typename T, int TC, int KAHAN>
 static cudaError_t launch_prune_t(const PruneArgs &a, cudaStream_t s, int grid)
 {
     size_t smem = PruneSmem<T, TC>::bytes(a.nslots, a.nl, a.n_internal);
@@ -511,12 +542,13 @@ static cudaError_t launch_prune_t(const PruneArgs &a, cudaStream_t s, int grid)
     return cudaGetLastError();
 }
 
-cudaError_t launch_prune(int prec, bool compensated, const PruneArgs &a, cudaStream_t s, int grid)
+cudaError_t launch_prune(int prec, int comp, const PruneArgs &a, cudaStream_t s, int grid)
 {
     if (a.nwi <= 0) return cudaSuccess;
-    if (prec == PCSF_PREC_FP64) return launch_prune_t<double, 32, false>(a, s, grid);
-    if (compensated) return launch_prune_t<float, 64, true>(a, s, grid);
-    return launch_prune_t<float, 64, false>(a, s, grid);
+    if (prec == PCSF_PREC_FP64) return launch_prune_t<double, 32, 0>(a, s, grid);
+    if (comp == 1) return launch_prune_t<float, 64, 1>(a, s, grid);
+    if (comp == 2) return launch_prune_t<float, 64, 2>(a, s, grid);
+    return launch_prune_t<float, 64, 0>(a, s, grid);
 }
 
 // ---------------------------------------------------------------------------

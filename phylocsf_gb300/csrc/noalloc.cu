@@ -151,8 +151,8 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
         pa.m = m;
         pa.partials = d_part;
         const bool tcprec = prec == PCSF_PREC_TF32X3 || prec == PCSF_PREC_TF32;
-        ce = launch_prune(prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32, comp != 0 || tcprec, pa, s,
-                          std::min(pgrid, nwi));
+        ce = launch_prune(prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32, (comp == 0 && tcprec) ? 1 : comp, pa,
+                          s, std::min(pgrid, nwi));
     }
     if (ce == cudaSuccess) ce = launch_reduce(d_part, d_wib, n_regions, d_lpr, d_elpr_out, s);
     int32_t key = STATUS_NONE;

@@ -83,6 +83,7 @@ cudaError_t launch_jacobi(const double *A, double *U, double *lam, int *status, 
 cudaError_t launch_pform(bool fp64, const PSet *ps, int nps, const double *branch, int nbr,
                          DevModels m, void *Pbuf, int32_t *status_key, cudaStream_t s, bool raw = false);
 cudaError_t launch_d2f(const double *in, float *out, size_t n, cudaStream_t s);
+cudaError_t launch_d2f_rows(const double *in, float *out, size_t nmat, cudaStream_t s);
 
 // Pruning over work items [nwi]; partials [nwi][2] (lpr, elpr).
 struct PruneArgs {
@@ -99,7 +100,8 @@ struct PruneArgs {
     DevModels m;
     double *partials;        // [nwi][2]
 };
-cudaError_t launch_prune(int prec, bool compensated, const PruneArgs &a, cudaStream_t s, int grid);
+// comp: 0 plain FP32 sums, 1 Kahan, 2 blocked Kahan (see prune_common.cuh)
+cudaError_t launch_prune(int prec, int comp, const PruneArgs &a, cudaStream_t s, int grid);
 int prune_tile_cols(int prec);
 size_t prune_smem_bytes(int prec, int nslots, int nl, int nint);
 
@@ -123,7 +125,7 @@ struct GradArgs {
     double *partials;        // [nwi][2]
     double *gpart;           // [nwi][nbr]
 };
-cudaError_t launch_grad(int prec, bool compensated, const GradArgs &a, cudaStream_t s, int grid);
+cudaError_t launch_grad(int prec, int comp, const GradArgs &a, cudaStream_t s, int grid);
 size_t grad_scratch_per_cta(int prec, int nl);
 size_t grad_smem_bytes(int prec, int nslots, int nl, int nint);
 cudaError_t launch_reduce_grad(const double *gpart, const int32_t *wi_begin, int nreq, int nbr, double *grad,

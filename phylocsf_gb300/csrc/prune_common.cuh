@@ -63,9 +63,13 @@ __device__ inline float scale2(float x, int e) { return ldexpf(x, e); }
 __device__ inline double scale2(double x, int e) { return ldexp(x, e); }
 
 // out[i][cc] = sum_j M[j][a0+i] * X[j][c0+cc] for a 64 x TC shared-memory tile
-// X ([K][TC]) and a 64 x 64 matrix M ([K][K], row j contiguous), optionally
-// with compensated summation.
-template <typename T, int TC, bool KAHAN>
+// X ([K][TC]) and a 64 x 64 matrix M ([K][K], row j contiguous).
+// COMP selects the summation: 0 plain FP32 (products smaller than half an ulp of
+// the running sum are lost, a downward bias), 1 Kahan on every term, 2 blocked:
+// eight products summed plainly, then each block folded into the running sum
+// with Kahan's correction (about a ninth of the plain bias at 1.5 operations per
+// product instead of 5).
+template <typename T, int TC, int COMP>
 __device__ inline void contract(const T *M, const T *X, int a0, int c0, T out[4][TC / 16])
 {
     constexpr int CPT = TC / 16;
@@ -77,28 +81,58 @@ __device__ inline void contract(const T *M, const T *X, int a0, int c0, T out[4]
             out[i][cc] = (T)0;
             comp[i][cc] = (T)0;
         }
-#pragma unroll 4
-    for (int j = 0; j < K; j++) {
-        T e[4], x[CPT];
-        Vec4<T>::load(M + j * K + a0, e);
-        ColLoad<T, CPT>::load(X + j * TC + c0, x);
+    if (COMP == 2) {
+#pragma unroll 1
+        for (int jb = 0; jb < K; jb += 8) {
+            T g[4][CPT];
 #pragma unroll
-        for (int i = 0; i < 4; i++)
+            for (int i = 0; i < 4; i++)
 #pragma unroll
-            for (int cc = 0; cc < CPT; cc++) {
-                if (KAHAN) {
-                    // compensated summation: the rounding error of each addition is
-                    // carried in comp, so small terms are not lost against a large sum
-                    T y = e[i] * x[cc] - comp[i][cc];
+                for (int cc = 0; cc < CPT; cc++) g[i][cc] = (T)0;
+#pragma unroll
+            for (int j = jb; j < jb + 8; j++) {
+                T e[4], x[CPT];
+                Vec4<T>::load(M + j * K + a0, e);
+                ColLoad<T, CPT>::load(X + j * TC + c0, x);
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int cc = 0; cc < CPT; cc++) g[i][cc] += e[i] * x[cc];
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int cc = 0; cc < CPT; cc++) {
+                    T y = g[i][cc] - comp[i][cc];
                     T t = out[i][cc] + y;
                     comp[i][cc] = (t - out[i][cc]) - y;
                     out[i][cc] = t;
-                } else {
-                    out[i][cc] += e[i] * x[cc];
                 }
-            }
+        }
+    } else {
+#pragma unroll 4
+        for (int j = 0; j < K; j++) {
+            T e[4], x[CPT];
+            Vec4<T>::load(M + j * K + a0, e);
+            ColLoad<T, CPT>::load(X + j * TC + c0, x);
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int cc = 0; cc < CPT; cc++) {
+                    if (COMP == 1) {
+                        // compensated summation: the rounding error of each addition is
+                        // carried in comp, so small terms are not lost against a large sum
+                        T y = e[i] * x[cc] - comp[i][cc];
+                        T t = out[i][cc] + y;
+                        comp[i][cc] = (t - out[i][cc]) - y;
+                        out[i][cc] = t;
+                    } else {
+                        out[i][cc] += e[i] * x[cc];
+                    }
+                }
+        }
     }
-    if (KAHAN) {
+    if (COMP) {
 #pragma unroll
         for (int i = 0; i < 4; i++)
 #pragma unroll
@@ -109,7 +143,7 @@ __device__ inline void contract(const T *M, const T *X, int a0, int c0, T out[4]
 // Partial of child c at its parent: v[a] = alpha_c[a] + sum_j E_c[a][j] alpha_c[j]
 // (internal child, slot >= 0; Et = E_c^T) or the gather v[a] = P_c[a][s] of a
 // leaf in state s (1 for a marginalised leaf: P rows sum to 1).
-template <typename T, int TC, bool KAHAN>
+template <typename T, int TC, int KAHAN>
 __device__ inline void child_partial(const T *Et, const T *slots, int slot, int leaf, const uint8_t *lvT, int a0,
                                      int c0, T v[4][TC / 16])
 {

@@ -24,9 +24,10 @@
 // E^T rows from L2 while the MMAs run.  The per-column rescale exponent is the
 // maximum over the two threads of a column.
 //
-// Accuracy: the tensor cores' FP32 accumulation is not round-to-nearest (a
-// measured mean of -0.3 ulp per accumulation step of the 8-product chunks), so
-// these values carry a small systematic error.  The engine therefore uses this
+// Accuracy: the tensor cores' FP32 accumulation is not round-to-nearest: it
+// rounds toward minus infinity (a measured mean of -5.7 ulp of the result over
+// one K = 64 product, i.e. 8 accumulation steps, for positive and for negative
+// results alike), so these values carry a small systematic error.  The engine therefore uses this
 // kernel for the search evaluations of the rho maximisation and reports every
 // returned likelihood from the compensated FP32 kernel.
 //

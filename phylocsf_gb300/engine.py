@@ -28,6 +28,8 @@ STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memo
 FIXED, MLE = 0, 1
 PREC = {"fp64": 0, "fp32": 1, "tf32x3": 2, "bf16x3": 3, "tf32": 4,
         "fp32c": 1 | (1 << 16),      # FP32 contractions with compensated summation
+        "fp32b": 1 | (1 << 18),      # FP32 contractions with blocked compensation
+        "tf32x3b": 2 | (1 << 18),    # tensor-core search, blocked-compensation returned values
         "tf32x3_direct": 2 | (1 << 17), "tf32_direct": 4 | (1 << 17)}   # lpr straight from the tensor cores
 MARGINALIZE = 64
 ORF_MODES = {"asis": 0, "atgstop": 1, "stopstop": 2, "stopstop3": 3, "tofirststop": 4,

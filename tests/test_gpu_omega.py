@@ -1,9 +1,13 @@
 """OmegaModel test on the GPU (pcsf_omega_score) against the oracle restatement (oracle/omega.py).
 
-Tolerances: FP64 engine |d score| <= 1e-6 dB and kappa / rho within 1e-7
-relative (same iterates as the oracle); compensated-FP32 engine |d score| <=
-1e-2 dB (its P(t) is formed in FP64; the pruning is FP32 and the coordinate
-ascent may take different Brent steps).
+Tolerances: FP64 engine |d score| <= 1e-6 dB, and kappa / rho within 2 %
+relative.  The engine builds each Omega Q and its eigensystem on the GPU, so
+its likelihoods agree with the oracle's to ~1e-13 relative, not bit for bit; a
+Brent probe sqrt(eps)*|x| from the best point can then compare the other way,
+after which the coordinate ascent ends at another point inside its stopping
+rule (bracket width <= 1 % of the parameter) while the score, flat at the
+optimum, still agrees.  Compensated-FP32 engine |d score| <= 1e-2 dB (its P(t)
+is formed in FP64; the pruning is FP32).
 """
 import numpy as np
 import pytest
@@ -42,10 +46,12 @@ def test_omega_matches_oracle(prec):
         assert g["status"] == 0
         if prec == "fp64":
             assert abs(g["score"] - sc) <= 1e-6, (r, g["score"], sc)
-            assert g["kappa_h0"] == pytest.approx(q0[0], rel=1e-7)
-            assert g["rho_h0"] == pytest.approx(r0, rel=1e-7)
-            assert g["kappa_h1"] == pytest.approx(q1[0], rel=1e-7)
-            assert g["rho_h1"] == pytest.approx(r1, rel=1e-7)
+            assert g["kappa_h0"] == pytest.approx(q0[0], rel=2e-2)
+            assert g["rho_h0"] == pytest.approx(r0, rel=2e-2)
+            assert g["kappa_h1"] == pytest.approx(q1[0], rel=2e-2)
+            assert g["rho_h1"] == pytest.approx(r1, rel=2e-2)
+            assert g["lpr_h0"] == pytest.approx(l0, rel=1e-9)
+            assert g["lpr_h1"] == pytest.approx(l1, rel=1e-9)
         else:
             assert abs(g["score"] - sc) <= 1e-2, (r, g["score"], sc)
 
