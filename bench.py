@@ -38,6 +38,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "codon-column·branches/s and regions scored/s at |Δscore|≤1e-3 dB vs FP64 oracle"
 L2_BYTES = 129 * 1024 * 1024
+DTYPES = {"fp32": "f32", "fp32c": "f32 (compensated)", "fp32b": "f32 (blocked compensation)", "fp64": "f64",
+          "tf32x3": "tf32x3 search, f32 (compensated) reported",
+          "tf32x3b": "tf32x3 search, f32 (blocked compensation) reported"}
 
 
 def flops_per_column(nl: int) -> int:
@@ -304,13 +307,14 @@ def run_ours(args, world, rank, local):
 
     line = {"metric": METRIC, "value": value, "unit": "regions/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": {"fp32": "f32", "fp32c": "f32 (compensated)", "fp64": "f64"}.get(args.precision, args.precision),
+            "vs_baseline": None, "dtype": DTYPES.get(args.precision, args.precision),
             "data": "synthetic (seeded simulation along the tree; no public benchmark exists)",
             "config": {"workload": wl.name, "tree": ps.name, "strategy": "mle" if wl.strategy else "fixed",
                        "regions_per_gpu": wl.n_regions, "columns_per_gpu": wl.total_cols,
                        "precision": args.precision, "l2": ("L2 flushed before every timed step (inputs %.0f MB)" if flush is not None
                               else "inputs larger than L2 (%.0f MB)") % (wl.leaves.nbytes / 1e6),
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "ctas": {"simt_prune": st["prune_grid"], "tensor_core_prune": st["tc_grid"]}},
             "column_branches_per_s": colb_per_s,
             "e2e": {"value": e2e_value, "unit": "regions/s", "h2d_bytes_per_step": int(wl.leaves.nbytes +
                                                                                        wl.col_offsets.nbytes),
@@ -369,7 +373,7 @@ def main():
     ap.add_argument("--workload", default="58mammals_mle")
     ap.add_argument("--regions", type=int, default=10000)
     ap.add_argument("--cols", type=int, default=2_000_000)
-    ap.add_argument("--precision", default="fp32c")
+    ap.add_argument("--precision", default="tf32x3b")
     ap.add_argument("--strategy", default=None, choices=[None, "fixed", "mle"],
                     help="override the workload's strategy (fixed: one likelihood pass, used for profiling)")
     ap.add_argument("--fp64-regions", type=int, default=256)

@@ -68,6 +68,12 @@ extern "C" {
  * kernel's values instead of the compensated FP32 kernel's (precision study). */
 #define PCSF_TC_DIRECT (1 << 17)
 
+/* engine flag for the FP32 and tensor-core modes: form every P(t) in FP64 (as
+ * the FP64 engine does) and round it to FP32, re-forming each diagonal from its
+ * rounded row, instead of the FP32 grid correction.  Much slower (FP64 GEMMs);
+ * for accuracy studies. */
+#define PCSF_PT_FP64 (1 << 19)
+
 /* engine flags, bits 8..15: CUDA device ordinal + 1 (0 = the calling thread's
  * current device).  Every call on an engine runs on the engine's device. */
 #define PCSF_DEVICE(d) ((((int32_t)(d)) + 1) << 8)
@@ -109,6 +115,8 @@ typedef struct {
     double other_ms;             /* device time of the other kernels            */
     int64_t prune_launches;
     int64_t pform_launches;
+    int32_t prune_grid;     /* launch configuration (not counters): CTAs of the SIMT pruning kernel, */
+    int32_t tc_grid;        /* and of the tensor-core kernel (0 if the engine has none)              */
 } pcsf_stats;
 
 /* ---------------------------------------------------------------- engine */

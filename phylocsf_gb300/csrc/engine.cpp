@@ -103,6 +103,7 @@ struct pcsf_engine {
     bool compensated = false;
     bool block_comp = false;
     bool tc_direct = false;
+    bool pt64 = false;             // FP32 storage of FP64-formed P(t)
     int comp_mode() const { return compensated ? 1 : block_comp ? 2 : 0; }
     int accurate_comp() const { return block_comp ? 2 : 1; }
     bool has_models = false;
@@ -122,7 +123,7 @@ struct pcsf_engine {
 
     // device copies
     DevBuf<double> dU, dlam, dsq, disq, dwrow, dprior, dwlog, dbranch;
-    DevBuf<float> dUf, dgridT, dQf, dQ2f;
+    DevBuf<float> dUf, dgridT, dgrid_eg, dQf, dQ2f;
     DevBuf<double> dgrid_t;
     DevBuf<SchedNode> dsched;
     DevModels dm{};
@@ -130,6 +131,8 @@ struct pcsf_engine {
     // per-launch work buffers
     DevBuf<unsigned char> Pbuf;
     DevBuf<double> Pbuf64;
+    DevBuf<float> Bop;             // tensor-core B operands of the branches above internal nodes
+    int tc_grid = 0;
     size_t pbuf_psets = 0;
     DevBuf<PSet> dps;
     DevBuf<Request> dreq;
@@ -330,6 +333,13 @@ static int build_pt_grid(pcsf_engine *e, const double *Q[2])
         CK(launch_d2f(tmp.p, e->dgridT.p + (size_t)m * G * K2, (size_t)G * K2, e->stream), "grid convert");
         e->stats.kernel_launches += 2;
     }
+    std::vector<float> eg((size_t)2 * G * K);
+    for (int m = 0; m < 2; m++)
+        for (int g = 0; g < G; g++)
+            for (int mm = 0; mm < K; mm++) eg[((size_t)m * G + g) * K + mm] = (float)std::exp(e->lam[m][mm] * gt[g]);
+    CK(e->dgrid_eg.reserve((size_t)2 * G * K), "cudaMalloc");
+    CK(cudaMemcpyAsync(e->dgrid_eg.p, eg.data(), sizeof(float) * eg.size(), cudaMemcpyHostToDevice, e->stream),
+       "H2D grid");
     std::vector<float> qf(2 * K2), q2f(2 * K2);
     for (int m = 0; m < 2; m++)
         for (int i = 0; i < K; i++)
@@ -346,6 +356,7 @@ static int build_pt_grid(pcsf_engine *e, const double *Q[2])
     CK(cudaStreamSynchronize(e->stream), "P(t) grid");
     e->dm.gridT = e->dgridT.p;
     e->dm.grid_t = e->dgrid_t.p;
+    e->dm.grid_eg = e->dgrid_eg.p;
     e->dm.grid_n = G;
     e->dm.grid_lr = lr;
     e->dm.Qf = e->dQf.p;
@@ -463,6 +474,7 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
     e->compensated = (flags & PCSF_COMPENSATED) != 0;
     e->block_comp = (flags & PCSF_BLOCK_COMPENSATED) != 0;
     e->tc_direct = (flags & PCSF_TC_DIRECT) != 0;
+    e->pt64 = (flags & PCSF_PT_FP64) != 0;
     int ndev = 0;
     cudaError_t ce = cudaGetDeviceCount(&ndev);
     if (ce != cudaSuccess || ndev == 0)
@@ -490,10 +502,12 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
     CK(cudaMemsetAsync(e->derr.p, 0, sizeof(int), e->stream), "memset");
     const bool tc = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
     if (tc && !prune_tc_supported(e->nslots, e->nl))
-        return e->fail(PCSF_EINVAL, "tensor-core path supports up to 160 leaves and 6 partial slots (tree: %d, %d)",
+        return e->fail(PCSF_EINVAL, "tensor-core path supports up to 160 leaves and 8 partial slots (tree: %d, %d)",
                        e->nl, e->nslots);
-    if (tc && prune_tc_smem_bytes(e->nl) > (size_t)prop.sharedMemPerBlockOptin)
-        return e->fail(PCSF_EINVAL, "tensor-core path needs %zu B shared memory", prune_tc_smem_bytes(e->nl));
+    if (tc && prune_tc_smem_bytes(e->nl, (int)e->sched.size()) > (size_t)prop.sharedMemPerBlockOptin)
+        return e->fail(PCSF_EINVAL, "tensor-core path needs %zu B shared memory",
+                       prune_tc_smem_bytes(e->nl, (int)e->sched.size()));
+    if (tc) e->tc_grid = prop.multiProcessorCount * prune_tc_ctas_per_sm(e->nslots, e->nl, (int)e->sched.size());
     size_t smem = prune_smem_bytes(e->prec, e->nslots, e->nl, (int)e->sched.size());
     if (smem > (size_t)prop.sharedMemPerBlockOptin)
         return e->fail(PCSF_EINVAL, "tree needs %d partial slots (%zu B shared memory > %zu)", e->nslots, smem,
@@ -510,6 +524,7 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
     size_t freeb = 0, totalb = 0;
     CK(cudaMemGetInfo(&freeb, &totalb), "cudaMemGetInfo");
     size_t pset_bytes = (size_t)e->nbr * K2 * (e->prec == PCSF_PREC_FP64 ? 8 : 4);
+    if (tc) pset_bytes += (size_t)(e->nbr - e->nl) * 2 * K2 * sizeof(float);   // B operands
     size_t budget = std::min<size_t>(size_t(4) << 30, freeb / 4);
     e->pbuf_psets = std::max<size_t>(1, budget / pset_bytes);
     return PCSF_OK;
@@ -611,8 +626,12 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     for (size_t c = 0; c + 1 < chunk_ps_begin.size(); c++)
         max_chunk_ps = std::max<size_t>(max_chunk_ps, chunk_ps_begin[c + 1] - chunk_ps_begin[c]);
     CK(e->Pbuf.reserve(max_chunk_ps * pset_bytes), "cudaMalloc P(t) buffer");
-    const bool stage64 = dyn && e->prec != PCSF_PREC_FP64;   // FP64 formation, then FP32 storage
+    const bool stage64 = (dyn || e->pt64) && e->prec != PCSF_PREC_FP64;   // FP64 formation, then FP32 storage
     if (stage64) CK(e->Pbuf64.reserve(max_chunk_ps * (size_t)e->nbr * K2), "cudaMalloc P(t) staging buffer");
+    const int nbop = e->nbr - e->nl;
+    const bool want_bop = tc && !grad;
+    if (want_bop) CK(e->Bop.reserve(max_chunk_ps * (size_t)nbop * 2 * K2), "cudaMalloc tensor-core operand buffer");
+    float *bop = want_bop ? e->Bop.p : nullptr;
     size_t gscr = 0;
     if (grad) {
         gscr = grad_scratch_per_cta(e->prec, e->nl);
@@ -642,12 +661,12 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         if (stage64) {
             CK(launch_pform(true, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, dmv, e->Pbuf64.p, e->dstatus.p + p0, s),
                "P(t) formation launch");
-            CK(launch_d2f_rows(e->Pbuf64.p, reinterpret_cast<float *>(e->Pbuf.p), (size_t)(p1 - p0) * e->nbr, s),
-               "P(t) conversion launch");
+            CK(launch_d2f_rows(e->Pbuf64.p, reinterpret_cast<float *>(e->Pbuf.p), (size_t)(p1 - p0) * e->nbr, e->nbr,
+                               bop, e->nl, s), "P(t) conversion launch");
             e->stats.kernel_launches += 1;
         } else {
             CK(launch_pform(e->prec == PCSF_PREC_FP64 || dyn, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, dmv,
-                            e->Pbuf.p, e->dstatus.p + p0, s), "P(t) formation launch");
+                            e->Pbuf.p, e->dstatus.p + p0, s, false, bop, e->nl), "P(t) formation launch");
         }
         CK(cudaEventRecord(e->ev[1], s), "event");
         PruneArgs pa{};
@@ -663,6 +682,8 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         pa.nslots = e->nslots;
         pa.m = dmv;
         pa.partials = e->dpart.p + 2 * (size_t)wib[r0];
+        pa.Bop = bop;
+        pa.nbop = nbop;
         if (grad) {
             GradArgs ga{};
             ga.wi = pa.wi;
@@ -686,7 +707,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
             CK(launch_grad(e->prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32,
                            tce ? e->accurate_comp() : e->comp_mode(), ga, s, grid), "gradient launch");
         } else if (tc) {
-            int grid = std::min(e->sm_count, std::max(pa.nwi, 1));
+            int grid = std::min(e->tc_grid, std::max(pa.nwi, 1));
             CK(launch_prune_tc(e->prec == PCSF_PREC_TF32X3 ? 3 : 1, pa, e->derr.p, s, grid), "tensor-core pruning launch");
         } else {
             int grid = std::min(e->prune_grid, std::max(pa.nwi, 1));
@@ -1614,6 +1635,8 @@ int pcsf_engine_get_stats(const pcsf_engine *e, pcsf_stats *out)
 {
     if (!e || !out) return PCSF_EINVAL;
     *out = e->stats;
+    out->prune_grid = e->prune_grid;
+    out->tc_grid = e->tc_grid;
     return PCSF_OK;
 }
 

@@ -163,9 +163,24 @@ __device__ inline void status_min(int32_t *key, int branch, int row, int code)
     atomicMin(key, ((branch * K + row) << 4) | code);
 }
 
+// Tensor-core B operand of E (rows a, K = j): TF32 hi / lo parts in the K-major
+// core-matrix layout of the tensor-core kernel (tc_kernels.cu), 16 KB each:
+// element (a, j) at float offset (j/4)*256 + a*4 + j%4 of its part.
+__device__ __forceinline__ void bop_store(float *dst, int a, int q, float4 x)
+{
+    const float4 h = make_float4(__uint_as_float(__float_as_uint(x.x) & 0xFFFFE000u),
+                                 __uint_as_float(__float_as_uint(x.y) & 0xFFFFE000u),
+                                 __uint_as_float(__float_as_uint(x.z) & 0xFFFFE000u),
+                                 __uint_as_float(__float_as_uint(x.w) & 0xFFFFE000u));
+    const float4 l = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
+    *reinterpret_cast<float4 *>(dst + q * 256 + a * 4) = h;
+    *reinterpret_cast<float4 *>(dst + K2 + q * 256 + a * 4) = l;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const double *branch, int nbr,
-                                                       DevModels m, T *Pbuf, int32_t *status_key, int raw)
+                                                       DevModels m, T *Pbuf, int32_t *status_key, int raw,
+                                                       float *Bop, int bop_nl)
 {
     extern __shared__ __align__(16) unsigned char psm[];
     T *UT = reinterpret_cast<T *>(psm);     // [K][K]   UT[m][j] = U[j][m]
@@ -222,12 +237,21 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
         __syncthreads();
         const int mode = mode_s;
         if (tid < K) {
-            ex[tid] = expm1(lam[tid] * t);
-            if (mode == 3) {
-                const double tg = m.grid_t[grid_s];
-                cf[tid] = exp(lam[tid] * tg) * expm1(lam[tid] * (t - tg));
-            } else {
+            // ex feeds the row-sum check, which needs it only where w_m != 0
+            // (the stationary direction); the FP32 modes therefore spend one
+            // FP64 expm1 per branch instead of 64 (FP64 is a narrow pipe here).
+            if (mode == 0) {
+                ex[tid] = expm1(lam[tid] * t);
                 cf[tid] = ex[tid];
+            } else {
+                ex[tid] = (wrow[tid] != 0.0) ? expm1(lam[tid] * t) : 0.0;
+                if (mode == 3) {
+                    // e^{lam t_g} (tabulated) * expm1(lam (t - t_g)) in FP32: the
+                    // coefficient is rounded to FP32 for the GEMM in any case
+                    const double h = t - m.grid_t[grid_s];
+                    const float eg = m.grid_eg[((size_t)md * m.grid_n + grid_s) * K + tid];
+                    cf[tid] = (double)(eg * expm1f((float)(lam[tid] * h)));
+                }
             }
         }
         __syncthreads();
@@ -279,12 +303,12 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
                 if (w != 0.0) rs += U[i * K + mm] * ex[mm] * w;
             }
             rs *= isq[i];
-            // the diagonal is the FP64 sum of the stored (rounded) off-diagonal
-            // entries, so every stored row of P = I + E sums to 1 to within one
-            // rounding of the diagonal; a plain FP32 sum here biases lpr by
-            // ~1e-4 nats per 3000 codons at rho = 1
+            // the diagonal is the compensated sum of the stored (rounded)
+            // off-diagonal entries, so every stored row of P = I + E sums to 1
+            // to within one rounding of the diagonal; a plain FP32 sum here
+            // biases lpr by ~1e-4 nats per 3000 codons at rho = 1
             bool neg = false;
-            double diag = 0.0;
+            T diag = (T)0, dc = (T)0;
             for (int j = 0; j < K; j++) {
                 T x = Es[i * (K + 1) + j];
                 if (j == i) {
@@ -296,12 +320,19 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
                     x = (T)0;
                     Es[i * (K + 1) + j] = x;
                 }
-                diag -= (double)x;
+                if (fp32) {           // Kahan: diag -= x
+                    const T y = -x - dc;
+                    const T tt = diag + y;
+                    dc = (tt - diag) - y;
+                    diag = tt;
+                } else {
+                    diag -= x;
+                }
             }
             if (neg) status_min(status_key + r, b, i, PCSF_ENEGP);
             else if (fabs(rs) > m.tol) status_min(status_key + r, b, i, PCSF_EROWSUM);
-            else if (!(diag > -1.0)) status_min(status_key + r, b, i, PCSF_EDIAG);
-            Es[i * (K + 1) + i] = (T)diag;
+            else if (!((double)diag > -1.0)) status_min(status_key + r, b, i, PCSF_EDIAG);
+            Es[i * (K + 1) + i] = diag;
         }
         __syncthreads();
         T *out = Pbuf + ((size_t)r * nbr + b) * K2;
@@ -309,11 +340,19 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
             int j = f / K, i = f % K;
             out[f] = Es[i * (K + 1) + j];
         }
+        if (fp32 && Bop && b >= bop_nl) {      // branch above an internal node: tensor-core operand too
+            float *dst = Bop + ((size_t)r * (nbr - bop_nl) + (b - bop_nl)) * 2 * K2;
+            for (int f = tid; f < K2 / 4; f += PF_THREADS) {
+                const int a = f & (K - 1), q = f >> 6;
+                const T *row = Es + a * (K + 1) + 4 * q;
+                bop_store(dst, a, q, make_float4((float)row[0], (float)row[1], (float)row[2], (float)row[3]));
+            }
+        }
     }
 }
 
 cudaError_t launch_pform(bool fp64, const PSet *req, int nreq, const double *branch, int nbr, DevModels m,
-                         void *Pbuf, int32_t *status_key, cudaStream_t s, bool raw)
+                         void *Pbuf, int32_t *status_key, cudaStream_t s, bool raw, float *bop, int bop_nl)
 {
     if (nreq <= 0) return cudaSuccess;
     dim3 grid((nbr + PF_BRANCHES - 1) / PF_BRANCHES, nreq);
@@ -321,14 +360,16 @@ cudaError_t launch_pform(bool fp64, const PSet *req, int nreq, const double *bra
         size_t smem = sizeof(double) * (2 * K2 + K * (K + 1) + 4 * K);
         cudaError_t e = cudaFuncSetAttribute(k_pform<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k_pform<double><<<grid, PF_THREADS, smem, s>>>(req, branch, nbr, m, (double *)Pbuf, status_key, raw ? 1 : 0);
+        k_pform<double><<<grid, PF_THREADS, smem, s>>>(req, branch, nbr, m, (double *)Pbuf, status_key, raw ? 1 : 0,
+                                                       nullptr, 0);
     } else {
         size_t smem = sizeof(float) * (2 * K2 + K * (K + 1) + 2 * K);
         smem = (smem + 15) & ~size_t(15);
         smem += sizeof(double) * 2 * K;
         cudaError_t e = cudaFuncSetAttribute(k_pform<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k_pform<float><<<grid, PF_THREADS, smem, s>>>(req, branch, nbr, m, (float *)Pbuf, status_key, raw ? 1 : 0);
+        k_pform<float><<<grid, PF_THREADS, smem, s>>>(req, branch, nbr, m, (float *)Pbuf, status_key, raw ? 1 : 0,
+                                                      bop, bop_nl);
     }
     return cudaGetLastError();
 }
@@ -348,7 +389,10 @@ cudaError_t launch_d2f(const double *in, float *out, size_t n, cudaStream_t s)
 // FP64 -> FP32 for E^T matrices that already obey the row rule: off-diagonal
 // entries are rounded and each diagonal is re-formed as the FP64 sum of its
 // row's rounded entries (storage E^T: element (i, j) of E at [j*K + i]).
-__global__ void __launch_bounds__(256) k_d2f_rows(const double *in, float *out, size_t nmat)
+// Matrices are [set][nbr]; with bop, the branches b >= bop_nl also get their
+// tensor-core B operand (see bop_store).
+__global__ void __launch_bounds__(256) k_d2f_rows(const double *in, float *out, size_t nmat, int nbr, float *bop,
+                                                  int bop_nl)
 {
     const size_t mat = blockIdx.x * (size_t)4 + threadIdx.x / K;
     const int i = threadIdx.x % K;
@@ -363,12 +407,19 @@ __global__ void __launch_bounds__(256) k_d2f_rows(const double *in, float *out, 
         d -= (double)x;
     }
     dst[i * K + i] = (float)d;
+    const int b = (int)(mat % (size_t)nbr);
+    if (bop && b >= bop_nl) {
+        float *bd = bop + ((mat / nbr) * (size_t)(nbr - bop_nl) + (b - bop_nl)) * 2 * K2;
+        for (int q = 0; q < K / 4; q++)
+            bop_store(bd, i, q, make_float4(dst[(4 * q) * K + i], dst[(4 * q + 1) * K + i], dst[(4 * q + 2) * K + i],
+                                            dst[(4 * q + 3) * K + i]));
+    }
 }
 
-cudaError_t launch_d2f_rows(const double *in, float *out, size_t nmat, cudaStream_t s)
+cudaError_t launch_d2f_rows(const double *in, float *out, size_t nmat, int nbr, float *bop, int bop_nl, cudaStream_t s)
 {
     if (nmat == 0) return cudaSuccess;
-    k_d2f_rows<<<(unsigned)((nmat + 3) / 4), 256, 0, s>>>(in, out, nmat);
+    k_d2f_rows<<<(unsigned)((nmat + 3) / 4), 256, 0, s>>>(in, out, nmat, nbr, bop, bop_nl);
     return cudaGetLastError();
 }
 

@@ -59,6 +59,7 @@ struct DevModels {
     // in FP64; below the first grid point E(t) = t Q + t^2/2 Q^2.
     const float *gridT;     // [2][G][K][K]  E(t_g)^T in FP32
     const double *grid_t;   // [G]
+    const float *grid_eg;   // [2][G][K]     e^{lam_m t_g}
     int grid_n;
     double grid_lr;         // log of the grid ratio
     const float *Qf;        // [2][K][K]  Q (row-major)
@@ -80,10 +81,13 @@ cudaError_t launch_jacobi(const double *A, double *U, double *lam, int *status, 
 // P(t) formation for P sets [nps]: writes E^T = (P - I)^T per branch into
 // Pbuf ([nps][nbr][K][K], element (j,i) = E[i][j]) in FP64 or FP32.
 // raw = true skips the row rule (used to form the FP64 grid itself).
+// bop (FP32 only, may be null): tensor-core B operands, [set][nbr - bop_nl][hi, lo][64 x 64],
+// of the branches b >= bop_nl (the branches above internal nodes when bop_nl = n_leaves)
 cudaError_t launch_pform(bool fp64, const PSet *ps, int nps, const double *branch, int nbr,
-                         DevModels m, void *Pbuf, int32_t *status_key, cudaStream_t s, bool raw = false);
+                         DevModels m, void *Pbuf, int32_t *status_key, cudaStream_t s, bool raw = false,
+                         float *bop = nullptr, int bop_nl = 0);
 cudaError_t launch_d2f(const double *in, float *out, size_t n, cudaStream_t s);
-cudaError_t launch_d2f_rows(const double *in, float *out, size_t nmat, cudaStream_t s);
+cudaError_t launch_d2f_rows(const double *in, float *out, size_t nmat, int nbr, float *bop, int bop_nl, cudaStream_t s);
 
 // Pruning over work items [nwi]; partials [nwi][2] (lpr, elpr).
 struct PruneArgs {
@@ -99,6 +103,8 @@ struct PruneArgs {
     int nslots;
     DevModels m;
     double *partials;        // [nwi][2]
+    const void *Bop;         // tensor-core kernel: per chunk-local P set, [nbop][hi, lo][64 x 64] B operands
+    int nbop;                //   of the branches above internal nodes (node nl + k)
 };
 // comp: 0 plain FP32 sums, 1 Kahan, 2 blocked Kahan (see prune_common.cuh)
 cudaError_t launch_prune(int prec, int comp, const PruneArgs &a, cudaStream_t s, int grid);
@@ -133,8 +139,9 @@ cudaError_t launch_reduce_grad(const double *gpart, const int32_t *wi_begin, int
 
 // Tensor-core pruning (tc_kernels.cu): nprod 3 = TF32 hi/lo split, 1 = single TF32.
 cudaError_t launch_prune_tc(int nprod, const PruneArgs &a, int *err, cudaStream_t s, int grid);
-size_t prune_tc_smem_bytes(int nl);
+size_t prune_tc_smem_bytes(int nl, int nint);
 bool prune_tc_supported(int nslots, int nl);
+int prune_tc_ctas_per_sm(int nslots, int nl, int nint);
 
 // Sum the partials of each request's contiguous work items in fixed order.
 cudaError_t launch_reduce(const double *partials, const int32_t *wi_begin, int nreq, double *out_lpr,

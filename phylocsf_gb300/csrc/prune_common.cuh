@@ -57,10 +57,38 @@ template <> struct ColLoad<double, 4> {
     static __device__ inline void load(const double *p, double v[4]) { Vec4<double>::load(p, v); }
 };
 
-__device__ inline int exp_of(float x) { int e; frexpf(x, &e); return e; }
-__device__ inline int exp_of(double x) { int e; frexp(x, &e); return e; }
-__device__ inline float scale2(float x, int e) { return ldexpf(x, e); }
-__device__ inline double scale2(double x, int e) { return ldexp(x, e); }
+// exp_of(x): the e of frexp (x = m 2^e, m in [0.5, 1)) read from the exponent
+// field for normal x; frexp itself for zero, subnormals and non-finite x.
+__device__ __forceinline__ int exp_of(float x)
+{
+    const int b = (__float_as_int(x) >> 23) & 0xff;
+    if (b != 0 && b != 0xff) return b - 126;
+    int e;
+    frexpf(x, &e);
+    return e;
+}
+__device__ __forceinline__ int exp_of(double x)
+{
+    const int b = (int)((__double_as_longlong(x) >> 52) & 0x7ff);
+    if (b != 0 && b != 0x7ff) return b - 1022;
+    int e;
+    frexp(x, &e);
+    return e;
+}
+// scale2(x, e) = x * 2^e as two multiplications by exact powers of two (e split
+// in halves of equal sign, so the intermediate lies between x and the result):
+// exact, like ldexp, whenever x and the result are normal or zero; |e| <= 252
+// (float) / 2044 (double), far beyond the per-node rescales.
+__device__ __forceinline__ float scale2(float x, int e)
+{
+    const int e1 = e >> 1, e2 = e - e1;
+    return x * __int_as_float((e1 + 127) << 23) * __int_as_float((e2 + 127) << 23);
+}
+__device__ __forceinline__ double scale2(double x, int e)
+{
+    const int e1 = e >> 1, e2 = e - e1;
+    return x * __longlong_as_double((long long)(e1 + 1023) << 52) * __longlong_as_double((long long)(e2 + 1023) << 52);
+}
 
 // out[i][cc] = sum_j M[j][a0+i] * X[j][c0+cc] for a 64 x TC shared-memory tile
 // X ([K][TC]) and a 64 x 64 matrix M ([K][K], row j contiguous).

@@ -15,42 +15,50 @@
 //
 // Layout: 256 threads; thread t owns tile column (site) t % 128, i.e. TMEM lane
 // t % 128, and states 32*(t/128) .. +31 (warp w reaches lanes 32*(w%4)..).
-// TMEM (512 columns x 128 lanes x 32 bit): D_l cols [0,64), D_r [64,128), and
-// up to six parked partials alpha (64 columns each) from col 128.  Shared memory
-// holds the MMA operands in the K-major no-swizzle core-matrix layout (8 rows x
-// 16 bytes per core matrix), written with 16-byte stores so that a warp covers
-// one contiguous 512-byte run: A (alpha, 128 x 64) hi/lo for two children and B
-// (E row-major, 64 x 64) hi/lo for two children.  Leaf children are gathers of
-// E^T rows from L2 while the MMAs run.  The per-column rescale exponent is the
-// maximum over the two threads of a column.
+// Tensor memory holds only the partial slots (64 columns each).  A child's
+// partial alpha_c is copied into the A operand (shared memory, hi and lo parts,
+// from which alpha_c = hi + lo exactly), so the MMA writes D_c over the child's
+// own slot; the epilogue reads alpha_c back from the A operand.  With
+// nslots * 64 <= 256 columns two CTAs share an SM.
+//
+// Shared memory (about 106 KB for 58 leaves): one A operand (128 x 64, hi + lo),
+// one B operand (64 x 64, hi + lo), the tile's leaf states and the schedule.
+// The two children of a node are contracted one after the other through the
+// same operand buffers.  B operands are pre-split by the P(t) kernel into this
+// exact layout, so one elected thread fetches each with a single 32 KB bulk copy
+// (cp.async.bulk, completion on an mbarrier), issued as soon as the previous
+// contraction has released the buffer.  Leaf children are gathers of E^T rows
+// from L2 while the MMAs run.  The per-column rescale exponent is the maximum
+// over the two threads of a column.
 //
 // Accuracy: the tensor cores' FP32 accumulation is not round-to-nearest: it
 // rounds toward minus infinity (a measured mean of -5.7 ulp of the result over
 // one K = 64 product, i.e. 8 accumulation steps, for positive and for negative
-// results alike), so these values carry a small systematic error.  The engine therefore uses this
-// kernel for the search evaluations of the rho maximisation and reports every
-// returned likelihood from the compensated FP32 kernel.
+// results alike), so these values carry a small systematic error.  The engine
+// therefore uses this kernel for the search evaluations of the rho maximisation
+// and reports every returned likelihood from the compensated FP32 kernel.
 //
 // Every mbarrier wait is bounded; on timeout the kernel records an error, waits
-// (again bounded) for its tensor-core work, releases its tensor memory and exits.
+// (again bounded) for its outstanding copies and tensor-core work, releases its
+// tensor memory and exits.
 #include <cmath>
 #include <cstdint>
 
 #include "pcsf_internal.h"
+#include "prune_common.cuh"
 
 namespace pcsf {
 
 constexpr int TCP_THREADS = 256;     // two threads per tile column
 constexpr int TCP_M = 128;
-constexpr int TCP_MAX_SLOTS = 6;
+constexpr int TCP_MAX_SLOTS = 8;     // 8 x 64 = all 512 tensor-memory columns
 constexpr int TCP_MAX_LEAVES = 160;
-constexpr uint32_t TCP_TMEM_COLS = 512;
 constexpr long TCP_WAIT_LIMIT = 1L << 22;
 
-// shared-memory map (bytes)
-constexpr uint32_t SM_A = 0;            // [2 children][hi,lo][128 x 64 fp32] = 4 x 32 KB
-constexpr uint32_t SM_B = 131072;       // [2 children][hi,lo][64 x 64 fp32]  = 4 x 16 KB
-constexpr uint32_t SM_LV = 196608;      // [nl][128] leaf states
+// dynamic shared-memory map (bytes)
+constexpr uint32_t SM_A = 0;            // [hi, lo][128 x 64 fp32] = 2 x 32 KB
+constexpr uint32_t SM_B = 65536;        // [hi, lo][64 x 64 fp32]  = 2 x 16 KB
+constexpr uint32_t SM_LV = 98304;       // [nl][128] leaf states, then the schedule
 constexpr uint32_t A_BYTES = 32768, B_BYTES = 16384;
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -114,18 +122,41 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
     return done != 0;
 }
 
+// one 32 KB bulk copy (B hi + lo) global -> shared, completing on mbarrier bar
+__device__ __forceinline__ void bulk_load_b(uint32_t dst, const void *src, uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(2 * B_BYTES) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(dst), "l"(src), "r"(2 * B_BYTES), "r"(bar) : "memory");
+}
+
 __device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
 
+// alpha = hi + lo of this thread's 32 states, read back from the A operand
+__device__ __forceinline__ void load_alpha(const unsigned char *sm, int site, int s0, int q, float *x)
+{
+#pragma unroll
+    for (int j4 = 0; j4 < 4; j4++) {
+        const uint32_t o = core_off(site, s0 + 16 * q + 4 * j4, 16);
+        const float4 h = *reinterpret_cast<const float4 *>(sm + SM_A + o);
+        const float4 l = *reinterpret_cast<const float4 *>(sm + SM_A + A_BYTES + o);
+        x[4 * j4 + 0] = h.x + l.x;
+        x[4 * j4 + 1] = h.y + l.y;
+        x[4 * j4 + 2] = h.z + l.z;
+        x[4 * j4 + 3] = h.w + l.w;
+    }
+}
+
 template <int NPROD>
-__global__ void __launch_bounds__(TCP_THREADS, 1) k_prune_tc(PruneArgs a, int *err)
+__global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32_t tmem_cols, int *err)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
     __shared__ uint32_t tbase_s;
-    __shared__ __align__(8) uint64_t bar;
-    __shared__ SchedNode sched[TCP_MAX_LEAVES];
-    __shared__ float cmax[2][TCP_M];
-    __shared__ double zpart[2][2][TCP_M];
+    __shared__ __align__(8) uint64_t bar_mma, bar_b;
+    __shared__ float cmax[2][2][TCP_M];
     __shared__ double red_l[TCP_THREADS / 32], red_e[TCP_THREADS / 32];
+    __shared__ int16_t bseq[TCP_MAX_LEAVES];     // internal children in contraction order
+    __shared__ int nbseq_s;
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int site = tid & (TCP_M - 1);          // tile column = TMEM lane
@@ -133,24 +164,132 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_prune_tc(PruneArgs a, int *e
     const int s0 = 32 * half;
     const int nl = a.nl;
     uint8_t *lvT = sm + SM_LV;
-    const uint32_t barA = smem_addr(&bar);
+    SchedNode *sched = reinterpret_cast<SchedNode *>(sm + SM_LV + ((nl * TCP_M + 15) & ~15));
+    const uint32_t barM = smem_addr(&bar_mma), barB = smem_addr(&bar_b);
+    const uint32_t sA = smem_addr(sm + SM_A), sB = smem_addr(sm + SM_B);
     // kind::tf32, D f32, A/B tf32, both K-major, N = 64, M = 128
     const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+    const float *Bop = reinterpret_cast<const float *>(a.Bop);
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     :: "r"(smem_addr(&tbase_s)), "r"(TCP_TMEM_COLS));
+                     :: "r"(smem_addr(&tbase_s)), "r"(tmem_cols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(barA), "r"(1));
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(barM), "r"(1));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(barB), "r"(1));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        int k = 0;
+        for (int f = 0; f < a.n_internal; f++) {
+            const SchedNode sn = a.sched[f];
+            if (sn.lslot >= 0) bseq[k++] = sn.lc;
+            if (sn.rslot >= 0) bseq[k++] = sn.rc;
+        }
+        nbseq_s = k;
+    }
     for (int f = tid; f < a.n_internal; f += TCP_THREADS) sched[f] = a.sched[f];
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tbase = tbase_s;
+    const int nbseq = nbseq_s;
     const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;   // warp w reaches lanes 32*(w%4)..
-    uint32_t phase = 0;
+    uint32_t ph_mma = 0, ph_b = 0;      // mbarrier parities (every thread tracks both)
+    // B loads: (work item, index into bseq) of the next load to issue; thread 0 only
+    int ld_w = blockIdx.x, ld_k = 0;
+    int b_inflight = 0;                 // loads issued and not yet waited for (thread 0)
     bool ok = true;
+
+    auto issue_next_b = [&]() {         // thread 0: the buffer is free
+        while (ld_w < a.nwi && ld_k >= nbseq) { ld_w += gridDim.x; ld_k = 0; }
+        if (ld_w >= a.nwi || nbseq == 0) return;
+        const int ps = a.req[a.wi[ld_w].request].pset;
+        const int c = bseq[ld_k++];
+        bulk_load_b(sB, Bop + ((size_t)ps * a.nbop + (c - nl)) * 2 * K2, barB);
+        b_inflight++;
+    };
+    if (tid == 0) issue_next_b();
+
+    // stage alpha of slot s (this thread's 32 states) as the A operand, hi and lo
+    auto stage_a = [&](int s) {
+        const uint32_t ts = tbase + lane_off + 64 * s + s0;
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            float x[16];
+            tmem_ld16(ts + 16 * q, x);
+#pragma unroll
+            for (int j4 = 0; j4 < 4; j4++) {
+                const float4 hv = make_float4(tf32_hi(x[4 * j4]), tf32_hi(x[4 * j4 + 1]), tf32_hi(x[4 * j4 + 2]),
+                                              tf32_hi(x[4 * j4 + 3]));
+                const float4 lv = make_float4(x[4 * j4] - hv.x, x[4 * j4 + 1] - hv.y, x[4 * j4 + 2] - hv.z,
+                                              x[4 * j4 + 3] - hv.w);
+                const uint32_t o = core_off(site, s0 + 16 * q + 4 * j4, 16);
+                *reinterpret_cast<float4 *>(sm + SM_A + o) = hv;
+                *reinterpret_cast<float4 *>(sm + SM_A + A_BYTES + o) = lv;
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    };
+    // thread 0: wait for the B operand
+    auto wait_b = [&]() -> bool {
+        if (!mbar_wait(barB, ph_b)) return false;
+        ph_b ^= 1u;
+        b_inflight--;
+        return true;
+    };
+    // thread 0, after the staging barrier: D (slot s) = A B
+    auto issue_mma = [&](int s) {
+        const uint32_t dt = tbase + 64 * s;
+        uint32_t acc = 0;
+        if (NPROD == 3) {
+            for (int k = 0; k < 8; k++) {
+                mma_tf32(dt, sdesc(sA + A_BYTES + k * 4096, 2048, 128), sdesc(sB + k * 2048, 1024, 128), idesc, acc);
+                acc = 1;
+                mma_tf32(dt, sdesc(sA + k * 4096, 2048, 128), sdesc(sB + B_BYTES + k * 2048, 1024, 128), idesc, 1);
+            }
+        }
+        for (int k = 0; k < 8; k++) {
+            mma_tf32(dt, sdesc(sA + k * 4096, 2048, 128), sdesc(sB + k * 2048, 1024, 128), idesc, acc);
+            acc = 1;
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                     :: "r"(barM) : "memory");
+    };
+    // v (or v *=) alpha + D for the internal child in slot s; A operand still holds alpha
+    auto child_value = [&](int s, float *v, bool mul) {
+        const uint32_t tD = tbase + lane_off + 64 * s + s0;
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            float d[16], x[16];
+            tmem_ld16(tD + 16 * q, d);
+            load_alpha(sm, site, s0, q, x);
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                const float u = x[j] + d[j];
+                v[16 * q + j] = mul ? v[16 * q + j] * u : u;
+            }
+        }
+    };
+    // leaf child: v (or v *=) P_c[a][s] = E^T[s][a] + (a == s), 1 if marginalised
+    auto leaf_value = [&](const float *Pc, int s, float *v, bool mul) {
+        const float4 *row = reinterpret_cast<const float4 *>(Pc + (size_t)(s < K ? s : 0) * K + s0);
+#pragma unroll
+        for (int j4 = 0; j4 < 8; j4++) {
+            float4 x = make_float4(1.f, 1.f, 1.f, 1.f);
+            if (s < K) {
+                x = __ldg(row + j4);
+                const int a0 = s0 + 4 * j4;
+                x.x += (s == a0) ? 1.0f : 0.0f;
+                x.y += (s == a0 + 1) ? 1.0f : 0.0f;
+                x.z += (s == a0 + 2) ? 1.0f : 0.0f;
+                x.w += (s == a0 + 3) ? 1.0f : 0.0f;
+            }
+            const float u[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+            for (int k = 0; k < 4; k++) v[4 * j4 + k] = mul ? v[4 * j4 + k] * u[k] : u[k];
+        }
+    };
 
     for (int w = blockIdx.x; w < a.nwi && ok; w += gridDim.x) {
         const WorkItem wi = a.wi[w];
@@ -164,159 +303,77 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_prune_tc(PruneArgs a, int *e
             int c = f / nl, l = f - c * nl;
             lvT[l * TCP_M + c] = (c < ncols) ? lg[f] : (uint8_t)K;
         }
+        __syncthreads();
         int escale = 0;     // this column's sum of rescale exponents
 
         for (int ni = 0; ni < a.n_internal && ok; ni++) {
             const SchedNode sn = sched[ni];
-            const int slot_of[2] = {sn.lslot, sn.rslot};
-            const int child[2] = {sn.lc, sn.rc};
-            const bool any_mma = slot_of[0] >= 0 || slot_of[1] >= 0;
-            // ---- stage B = E_c (row-major E[a][j]) hi / lo for internal children; float4 per (a, 4 j)
-#pragma unroll
-            for (int side = 0; side < 2; side++) {
-                if (slot_of[side] < 0) continue;
-                const float *g = Pbase + (size_t)child[side] * K2;   // E^T: g[j*64 + a] = E[a][j]
-                unsigned char *bh = sm + SM_B + side * 2 * B_BYTES;
-                unsigned char *bl = bh + B_BYTES;
-                for (int f = tid; f < 16 * K; f += TCP_THREADS) {
-                    const int aa = f & 63, q = f >> 6;
-                    float4 x;
-                    x.x = __ldg(g + (4 * q + 0) * K + aa);
-                    x.y = __ldg(g + (4 * q + 1) * K + aa);
-                    x.z = __ldg(g + (4 * q + 2) * K + aa);
-                    x.w = __ldg(g + (4 * q + 3) * K + aa);
-                    const float4 lo = make_float4(x.x - tf32_hi(x.x), x.y - tf32_hi(x.y), x.z - tf32_hi(x.z), x.w - tf32_hi(x.w));
-                    const uint32_t o = core_off(aa, 4 * q, 8);
-                    *reinterpret_cast<float4 *>(bh + o) = x;
-                    *reinterpret_cast<float4 *>(bl + o) = lo;
-                }
-            }
-            // ---- stage A = alpha_c (site-major) hi / lo from TMEM; this thread's 32 states
-#pragma unroll
-            for (int side = 0; side < 2; side++) {
-                if (slot_of[side] < 0) continue;
-                unsigned char *ah = sm + SM_A + side * 2 * A_BYTES;
-                unsigned char *al = ah + A_BYTES;
-                const uint32_t ts = tbase + lane_off + 128 + 64 * slot_of[side] + s0;
-#pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    float x[16];
-                    tmem_ld16(ts + 16 * q, x);
-#pragma unroll
-                    for (int j4 = 0; j4 < 4; j4++) {
-                        const float4 hv = make_float4(x[4 * j4], x[4 * j4 + 1], x[4 * j4 + 2], x[4 * j4 + 3]);
-                        const float4 lv = make_float4(hv.x - tf32_hi(hv.x), hv.y - tf32_hi(hv.y), hv.z - tf32_hi(hv.z),
-                                                      hv.w - tf32_hi(hv.w));
-                        const uint32_t o = core_off(site, s0 + 16 * q + 4 * j4, 16);
-                        *reinterpret_cast<float4 *>(ah + o) = hv;
-                        *reinterpret_cast<float4 *>(al + o) = lv;
-                    }
-                }
-            }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            tc_fence_before();
-            __syncthreads();
-            tc_fence_after();
-            if (tid == 0 && any_mma) {
-#pragma unroll
-                for (int side = 0; side < 2; side++) {
-                    if (slot_of[side] < 0) continue;
-                    const uint32_t dt = tbase + 64 * side;
-                    const uint32_t ah = smem_addr(sm + SM_A + side * 2 * A_BYTES), al = ah + A_BYTES;
-                    const uint32_t bh = smem_addr(sm + SM_B + side * 2 * B_BYTES), bl = bh + B_BYTES;
-                    uint32_t acc = 0;
-                    if (NPROD == 3) {
-                        for (int s = 0; s < 8; s++) {
-                            mma_tf32(dt, sdesc(al + s * 4096, 2048, 128), sdesc(bh + s * 2048, 1024, 128), idesc, acc);
-                            acc = 1;
-                            mma_tf32(dt, sdesc(ah + s * 4096, 2048, 128), sdesc(bl + s * 2048, 1024, 128), idesc, 1);
-                        }
-                    }
-                    for (int s = 0; s < 8; s++) {
-                        mma_tf32(dt, sdesc(ah + s * 4096, 2048, 128), sdesc(bh + s * 2048, 1024, 128), idesc, acc);
-                        acc = 1;
-                    }
-                }
-                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                             :: "r"(barA) : "memory");
-            }
-            // leaf children: gather E^T row s (L2) while the MMAs run
             float v[32];
-#pragma unroll
+            // internal children are contracted one after the other (l before r);
+            // leaf children are gathered while the last contraction runs.  Every
+            // barrier also agrees on a timed-out wait (bad), so that all threads
+            // leave together.
+            const int slotL = sn.lslot, slotR = sn.rslot;
+            const int nint = (slotL >= 0) + (slotR >= 0);
+            bool have = false, bad = false;
             for (int side = 0; side < 2; side++) {
-                if (slot_of[side] >= 0) continue;
-                const int s = lvT[child[side] * TCP_M + site];
-                const float4 *row = reinterpret_cast<const float4 *>(Pbase + (size_t)child[side] * K2 + (size_t)(s < K ? s : 0) * K + s0);
-#pragma unroll
-                for (int j4 = 0; j4 < 8; j4++) {
-                    float4 x = make_float4(1.f, 1.f, 1.f, 1.f);
-                    if (s < K) {
-                        x = __ldg(row + j4);
-                        const int a0 = s0 + 4 * j4;
-                        if (s >= a0 && s < a0 + 4) (&x.x)[s - a0] += 1.0f;
-                    }
-                    const float u[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-                    for (int k = 0; k < 4; k++) v[4 * j4 + k] = (side && slot_of[0] < 0) ? v[4 * j4 + k] * u[k] : u[k];
-                }
-            }
-            if (any_mma) {
-                bool done = mbar_wait(barA, phase);
-                phase ^= 1u;
-                if (__syncthreads_or(!done)) {
-                    if (tid == 0) atomicExch(err, 1);
-                    mbar_wait(barA, phase ^ 1u);   // a second bounded wait for the in-flight MMAs
-                    ok = false;
-                    break;
-                }
-            }
-            tc_fence_after();
-            // ---- epilogue: internal children v = alpha + D, product with the other child
-#pragma unroll
-            for (int side = 0; side < 2; side++) {
-                if (slot_of[side] < 0) continue;
-                const uint32_t tD = tbase + lane_off + 64 * side + s0;
-                const uint32_t tS = tbase + lane_off + 128 + 64 * slot_of[side] + s0;
-                // does v already hold the other child's partial?
-                const bool have_other = (side == 1) || (slot_of[1] < 0);
-#pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    float d[16], x[16];
-                    tmem_ld16(tD + 16 * q, d);
-                    tmem_ld16(tS + 16 * q, x);
-#pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        const float u = x[j] + d[j];
-                        v[16 * q + j] = have_other ? v[16 * q + j] * u : u;
+                const int s = side ? slotR : slotL;
+                if (s < 0) continue;
+                if (have && __syncthreads_or(bad)) { ok = false; break; }   // the A operand is free again
+                stage_a(s);
+                if (tid == 0 && !wait_b()) bad = true;
+                tc_fence_before();
+                if (__syncthreads_or(bad)) { ok = false; break; }
+                tc_fence_after();
+                if (tid == 0) issue_mma(s);
+                const bool last = (nint == 1) || side == 1;
+                if (last) {
+                    for (int ls = 0; ls < 2; ls++) {
+                        if ((ls ? slotR : slotL) >= 0) continue;
+                        const int c = ls ? sn.rc : sn.lc;
+                        leaf_value(Pbase + (size_t)c * K2, lvT[c * TCP_M + site], v, have);
+                        have = true;
                     }
                 }
+                const bool done = mbar_wait(barM, ph_mma);
+                ph_mma ^= 1u;
+                tc_fence_after();
+                if (!done) bad = true;
+                if (tid == 0 && done) issue_next_b();     // the B operand is free again
+                child_value(s, v, have);
+                have = true;
             }
+            if (!ok) break;
+            if (nint == 0) {
+                leaf_value(Pbase + (size_t)sn.lc * K2, lvT[sn.lc * TCP_M + site], v, false);
+                leaf_value(Pbase + (size_t)sn.rc * K2, lvT[sn.rc * TCP_M + site], v, true);
+            }
+            // ---- rescale by an exact power of two and park in the output slot
             float mx = 0.0f;
 #pragma unroll
             for (int k = 0; k < 32; k++) mx = fmaxf(mx, v[k]);
-            cmax[half][site] = mx;
-            __syncthreads();
-            mx = fmaxf(cmax[0][site], cmax[1][site]);
-            int e = 0;
-            if (mx > 0.0f) frexpf(mx, &e);
+            float (*cm)[TCP_M] = cmax[ni & 1];          // double-buffered: no second barrier needed
+            cm[half][site] = mx;
+            if (__syncthreads_or(bad)) { ok = false; break; }
+            mx = fmaxf(cm[0][site], cm[1][site]);
+            const int e = (mx > 0.0f) ? exp_of(mx) : 0;
             escale += e;
-            const uint32_t tO = tbase + lane_off + 128 + 64 * sn.oslot + s0;
+            const uint32_t tO = tbase + lane_off + 64 * sn.oslot + s0;
 #pragma unroll
             for (int q = 0; q < 2; q++) {
                 float y[16];
 #pragma unroll
-                for (int j = 0; j < 16; j++) y[j] = ldexpf(v[16 * q + j], -e);
+                for (int j = 0; j < 16; j++) y[j] = scale2(v[16 * q + j], -e);
                 tmem_st16(tO + 16 * q, y);
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-            tc_fence_before();
-            __syncthreads();
-            tc_fence_after();
         }
         if (!ok) break;
         // ---- root: z = alpha_root . prior, elpr term, FP64 sums over the tile
+        double *zpart = reinterpret_cast<double *>(sm + SM_A);   // [2][2][128]; the A operand is idle here
+        __syncthreads();
         {
-            const uint32_t tR = tbase + lane_off + 128 + 64 * sched[a.n_internal - 1].oslot + s0;
+            const uint32_t tR = tbase + lane_off + 64 * sched[a.n_internal - 1].oslot + s0;
             const double *pr = a.m.prior + md * K + s0;
             const double *wl = a.m.wlog + md * K + s0;
             double z = 0.0, wz = 0.0;
@@ -330,14 +387,14 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_prune_tc(PruneArgs a, int *e
                     wz += (double)x[j] * wl[16 * q + j];
                 }
             }
-            zpart[half][0][site] = z;
-            zpart[half][1][site] = wz;
+            zpart[(half * 2 + 0) * TCP_M + site] = z;
+            zpart[(half * 2 + 1) * TCP_M + site] = wz;
         }
         __syncthreads();
         double tl = 0.0, te = 0.0;
         if (half == 0 && site < ncols) {
-            const double z = zpart[0][0][site] + zpart[1][0][site];
-            const double wz = zpart[0][1][site] + zpart[1][1][site];
+            const double z = zpart[0 * TCP_M + site] + zpart[2 * TCP_M + site];
+            const double wz = zpart[1 * TCP_M + site] + zpart[3 * TCP_M + site];
             if (z > 0.0) {
                 tl = log(z) + (double)escale * 0.69314718055994530942;
                 te = wz / z;
@@ -360,28 +417,85 @@ __global__ void __launch_bounds__(TCP_THREADS, 1) k_prune_tc(PruneArgs a, int *e
             a.partials[2 * (size_t)w + 1] = se;
         }
     }
+    if (!ok && tid == 0) atomicExch(err, 1);
+    // quiesce: a bulk copy may be outstanding (loads run one ahead), and after a
+    // timed-out MMA wait its commit may still arrive; both waits are bounded
+    if (tid == 0) {
+        while (b_inflight > 0) {
+            if (!mbar_wait(barB, ph_b)) { atomicExch(err, 1); break; }
+            ph_b ^= 1u;
+            b_inflight--;
+        }
+    }
+    if (!ok) mbar_wait(barM, ph_mma);
     tc_fence_before();
     __syncthreads();
+    tc_fence_after();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tbase), "r"(TCP_TMEM_COLS));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tbase), "r"(tmem_cols));
 }
 
-size_t prune_tc_smem_bytes(int nl) { return SM_LV + (size_t)nl * TCP_M; }
+static uint32_t tmem_cols_for(int nslots)
+{
+    uint32_t need = (uint32_t)(64 * (nslots > 0 ? nslots : 1)), c = 32;
+    while (c < need) c <<= 1;
+    return c;
+}
+
+size_t prune_tc_smem_bytes(int nl, int nint)
+{
+    return SM_LV + (((size_t)nl * TCP_M + 15) & ~(size_t)15) + (size_t)nint * sizeof(SchedNode);
+}
 
 bool prune_tc_supported(int nslots, int nl) { return nslots <= TCP_MAX_SLOTS && nl <= TCP_MAX_LEAVES; }
+
+template <int NPROD>
+static cudaError_t set_tc_attributes(size_t smem)
+{
+    // the whole unified L1 as shared memory, so that two CTAs of ~110 KB fit
+    cudaError_t e = cudaFuncSetAttribute(k_prune_tc<NPROD>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_prune_tc<NPROD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return e;
+}
+
+// CTAs per SM: the smaller of what shared memory and registers allow (from the
+// kernel's attributes and the device limits) and what tensor memory allows
+int prune_tc_ctas_per_sm(int nslots, int nl, int nint)
+{
+    const uint32_t cols = tmem_cols_for(nslots);
+    const int by_tmem = (int)(512 / cols);
+    const size_t smem = prune_tc_smem_bytes(nl, nint);
+    cudaFuncAttributes fa;
+    int dev = 0, smem_sm = 0, regs_sm = 0, reserved = 0;
+    if (set_tc_attributes<3>(smem) != cudaSuccess || set_tc_attributes<1>(smem) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, k_prune_tc<3>) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess)
+        return 1;
+    const int by_smem = (int)((size_t)smem_sm / (fa.sharedSizeBytes + smem + (size_t)reserved));
+    const int by_regs = regs_sm / (fa.numRegs * TCP_THREADS);
+    int n = by_tmem;
+    if (by_smem < n) n = by_smem;
+    if (by_regs < n) n = by_regs;
+    return n > 0 ? n : 1;
+}
 
 cudaError_t launch_prune_tc(int nprod, const PruneArgs &a, int *err, cudaStream_t s, int grid)
 {
     if (a.nwi <= 0) return cudaSuccess;
-    size_t smem = prune_tc_smem_bytes(a.nl);
+    const size_t smem = prune_tc_smem_bytes(a.nl, a.n_internal);
+    const uint32_t cols = tmem_cols_for(a.nslots);
     if (nprod == 3) {
-        cudaError_t e = cudaFuncSetAttribute(k_prune_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = set_tc_attributes<3>(smem);
         if (e != cudaSuccess) return e;
-        k_prune_tc<3><<<grid, TCP_THREADS, smem, s>>>(a, err);
+        k_prune_tc<3><<<grid, TCP_THREADS, smem, s>>>(a, cols, err);
     } else {
-        cudaError_t e = cudaFuncSetAttribute(k_prune_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = set_tc_attributes<1>(smem);
         if (e != cudaSuccess) return e;
-        k_prune_tc<1><<<grid, TCP_THREADS, smem, s>>>(a, err);
+        k_prune_tc<1><<<grid, TCP_THREADS, smem, s>>>(a, cols, err);
     }
     return cudaGetLastError();
 }

@@ -30,7 +30,8 @@ PREC = {"fp64": 0, "fp32": 1, "tf32x3": 2, "bf16x3": 3, "tf32": 4,
         "fp32c": 1 | (1 << 16),      # FP32 contractions with compensated summation
         "fp32b": 1 | (1 << 18),      # FP32 contractions with blocked compensation
         "tf32x3b": 2 | (1 << 18),    # tensor-core search, blocked-compensation returned values
-        "tf32x3_direct": 2 | (1 << 17), "tf32_direct": 4 | (1 << 17)}   # lpr straight from the tensor cores
+        "tf32x3_direct": 2 | (1 << 17), "tf32_direct": 4 | (1 << 17),   # lpr straight from the tensor cores
+        "fp32b_pt64": 1 | (1 << 18) | (1 << 19)}   # FP64-formed P(t) stored in FP32 (accuracy studies)
 MARGINALIZE = 64
 ORF_MODES = {"asis": 0, "atgstop": 1, "stopstop": 2, "stopstop3": 3, "tofirststop": 4,
              "fromlaststop": 5, "toorfromstop": 6}
@@ -76,7 +77,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("kernel_launches", ctypes.c_int64), ("evaluations", ctypes.c_int64),
                 ("column_branches", ctypes.c_int64), ("rounds", ctypes.c_int64),
                 ("prune_ms", ctypes.c_double), ("pform_ms", ctypes.c_double), ("other_ms", ctypes.c_double),
-                ("prune_launches", ctypes.c_int64), ("pform_launches", ctypes.c_int64)]
+                ("prune_launches", ctypes.c_int64), ("pform_launches", ctypes.c_int64),
+                ("prune_grid", ctypes.c_int32), ("tc_grid", ctypes.c_int32)]
 
 
 # Every entry point declared in include/*.h, with its ctypes signature.

@@ -43,7 +43,9 @@ def _fast():
 
 
 @pytest.mark.parametrize("name,lengths", [("12flies", [300, 1, 127, 128, 129, 0, 7]),
-                                          ("58mammals", [50, 333, 1000, 3000])])
+                                          ("29mammals", [200, 129, 5]),
+                                          ("58mammals", [50, 333, 1000, 3000]),
+                                          ("120mammals", [150, 64])])
 def test_tensor_core_kernel_close_to_oracle(name, lengths):
     e = engine(name, "tf32x3_direct")
     mc, mn, ot, tree = H.oracle_models(name)
