@@ -132,6 +132,7 @@ struct pcsf_engine {
     DevBuf<unsigned char> Pbuf;
     DevBuf<double> Pbuf64;
     DevBuf<float> Bop;             // tensor-core B operands of the branches above internal nodes
+    DevBuf<float> dPfB;            // B operand of the tensor-core P(t) formation, per model
     int tc_grid = 0;
     size_t pbuf_psets = 0;
     DevBuf<PSet> dps;
@@ -443,6 +444,27 @@ static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2],
     e->dm.tol = e->tol;
     e->dm.grid_n = 0;
     e->has_models = true;
+    if (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32) {
+        // B operand of the tensor-core P(t) formation: B[j][m] = U_jm sqrt(pi_j), TF32 hi / lo,
+        // K-major core-matrix layout (element (j, m) at float (m/4)*256 + j*4 + m%4 of its part)
+        std::vector<float> bpf((size_t)2 * 2 * K2);
+        for (int m = 0; m < 2; m++)
+            for (int j = 0; j < K; j++)
+                for (int mm = 0; mm < K; mm++) {
+                    const float x = (float)(e->U[m][j * K + mm] * e->sq[m][j]);
+                    uint32_t bits;
+                    std::memcpy(&bits, &x, 4);
+                    bits &= 0xFFFFE000u;
+                    float hi;
+                    std::memcpy(&hi, &bits, 4);
+                    const size_t o = (size_t)m * 2 * K2 + (mm / 4) * 256 + j * 4 + mm % 4;
+                    bpf[o] = hi;
+                    bpf[o + K2] = x - hi;
+                }
+        CK(e->dPfB.reserve(bpf.size()), "cudaMalloc");
+        CK(cudaMemcpyAsync(e->dPfB.p, bpf.data(), sizeof(float) * bpf.size(), cudaMemcpyHostToDevice, e->stream), "H2D");
+        CK(cudaStreamSynchronize(e->stream), "model upload");
+    }
     {
         // Q row-major in both arithmetic types, for dP/dt = Q P(t) in the gradient
         std::vector<double> qd(2 * K2);
@@ -664,6 +686,10 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
             CK(launch_d2f_rows(e->Pbuf64.p, reinterpret_cast<float *>(e->Pbuf.p), (size_t)(p1 - p0) * e->nbr, e->nbr,
                                bop, e->nl, s), "P(t) conversion launch");
             e->stats.kernel_launches += 1;
+        } else if (want_bop && !dyn) {
+            CK(launch_pform_tc(e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, e->nl, dmv, e->dPfB.p,
+                               reinterpret_cast<float *>(e->Pbuf.p), bop, e->dstatus.p + p0, e->derr.p, s),
+               "tensor-core P(t) formation launch");
         } else {
             CK(launch_pform(e->prec == PCSF_PREC_FP64 || dyn, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, dmv,
                             e->Pbuf.p, e->dstatus.p + p0, s, false, bop, e->nl), "P(t) formation launch");

@@ -142,6 +142,11 @@ cudaError_t launch_prune_tc(int nprod, const PruneArgs &a, int *err, cudaStream_
 size_t prune_tc_smem_bytes(int nl, int nint);
 bool prune_tc_supported(int nslots, int nl);
 int prune_tc_ctas_per_sm(int nslots, int nl, int nint);
+// tensor-core P(t) formation for the search evaluations (tc_pform.cu): E^T of the
+// branches above leaves into Pbuf, B operands of the branches above internal
+// nodes into Bop; Bpf = per model the pre-split B = U^T D^1/2 [2][hi, lo][64 x 64]
+cudaError_t launch_pform_tc(const PSet *ps, int nps, const double *branch, int nbr, int nl, DevModels m,
+                            const float *Bpf, float *Pbuf, float *Bop, int32_t *status_key, int *err, cudaStream_t s);
 
 // Sum the partials of each request's contiguous work items in fixed order.
 cudaError_t launch_reduce(const double *partials, const int32_t *wi_begin, int nreq, double *out_lpr,

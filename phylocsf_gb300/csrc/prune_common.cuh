@@ -57,6 +57,26 @@ template <> struct ColLoad<double, 4> {
     static __device__ inline void load(const double *p, double v[4]) { Vec4<double>::load(p, v); }
 };
 
+// P(t) status keys: first error in (branch, row) order wins
+__device__ __forceinline__ void status_min(int32_t *key, int branch, int row, int code)
+{
+    atomicMin(key, ((branch * K + row) << 4) | code);
+}
+
+// Tensor-core B operand of E (rows a, K = j): TF32 hi / lo parts in the K-major
+// core-matrix layout of the tensor-core kernel (tc_kernels.cu), 16 KB each:
+// element (a, j) at float offset (j/4)*256 + a*4 + j%4 of its part.
+__device__ __forceinline__ void bop_store(float *dst, int a, int q, float4 x)
+{
+    const float4 h = make_float4(__uint_as_float(__float_as_uint(x.x) & 0xFFFFE000u),
+                                 __uint_as_float(__float_as_uint(x.y) & 0xFFFFE000u),
+                                 __uint_as_float(__float_as_uint(x.z) & 0xFFFFE000u),
+                                 __uint_as_float(__float_as_uint(x.w) & 0xFFFFE000u));
+    const float4 l = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
+    *reinterpret_cast<float4 *>(dst + q * 256 + a * 4) = h;
+    *reinterpret_cast<float4 *>(dst + K2 + q * 256 + a * 4) = l;
+}
+
 // exp_of(x): the e of frexp (x = m 2^e, m in [0.5, 1)) read from the exponent
 // field for normal x; frexp itself for zero, subnormals and non-finite x.
 __device__ __forceinline__ int exp_of(float x)

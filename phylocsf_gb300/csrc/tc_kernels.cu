@@ -46,6 +46,7 @@
 
 #include "pcsf_internal.h"
 #include "prune_common.cuh"
+#include "tc_common.cuh"
 
 namespace pcsf {
 
@@ -53,7 +54,6 @@ constexpr int TCP_THREADS = 256;     // two threads per tile column
 constexpr int TCP_M = 128;
 constexpr int TCP_MAX_SLOTS = 8;     // 8 x 64 = all 512 tensor-memory columns
 constexpr int TCP_MAX_LEAVES = 160;
-constexpr long TCP_WAIT_LIMIT = 1L << 22;
 
 // dynamic shared-memory map (bytes)
 constexpr uint32_t SM_A = 0;            // [hi, lo][128 x 64 fp32] = 2 x 32 KB
@@ -61,76 +61,6 @@ constexpr uint32_t SM_B = 65536;        // [hi, lo][64 x 64 fp32]  = 2 x 16 KB
 constexpr uint32_t SM_LV = 98304;       // [nl][128] leaf states, then the schedule
 constexpr uint32_t A_BYTES = 32768, B_BYTES = 16384;
 
-__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// byte offset of element (r, k) of a K-major tf32 operand with G = rows/8 row
-// groups: core matrix (g = r/8, q = k/4) at (q*G + g)*128, row r%8 at 16 B.
-__device__ __forceinline__ uint32_t core_off(int r, int k, int G)
-{
-    return (uint32_t)((((k >> 2) * G + (r >> 3)) << 7) + ((r & 7) << 4) + ((k & 3) << 2));
-}
-
-// shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
-// offsets between core matrices, descriptor version 1, no swizzle
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
-{
-    return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
-           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc)
-{
-    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                 " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
-                 :: "r"(dt), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
-{
-    uint32_t r[16];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-                 : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]);
-}
-
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float *v)
-{
-    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
-                 :: "r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
-                    "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
-                    "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
-                    "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
-                    "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
-                    "r"(__float_as_uint(v[15])));
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
-{
-    uint32_t done = 0;
-    for (long it = 0; it < TCP_WAIT_LIMIT && !done; it++) {
-        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-                     " selp.u32 %0, 1, 0, p;\n}\n"
-                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
-    }
-    return done != 0;
-}
-
-// one 32 KB bulk copy (B hi + lo) global -> shared, completing on mbarrier bar
-__device__ __forceinline__ void bulk_load_b(uint32_t dst, const void *src, uint32_t bar)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(2 * B_BYTES) : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 :: "r"(dst), "l"(src), "r"(2 * B_BYTES), "r"(bar) : "memory");
-}
-
-__device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
 
 // alpha = hi + lo of this thread's 32 states, read back from the A operand
 __device__ __forceinline__ void load_alpha(const unsigned char *sm, int site, int s0, int q, float *x)
@@ -206,7 +136,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
         if (ld_w >= a.nwi || nbseq == 0) return;
         const int ps = a.req[a.wi[ld_w].request].pset;
         const int c = bseq[ld_k++];
-        bulk_load_b(sB, Bop + ((size_t)ps * a.nbop + (c - nl)) * 2 * K2, barB);
+        bulk_load(sB, Bop + ((size_t)ps * a.nbop + (c - nl)) * 2 * K2, 2 * B_BYTES, barB);
         b_inflight++;
     };
     if (tid == 0) issue_next_b();
