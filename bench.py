@@ -44,7 +44,26 @@ DTYPES = {"fp32": "f32", "fp32c": "f32 (compensated)", "fp32b": "f32 (blocked co
 
 
 def flops_per_column(nl: int) -> int:
+    """One column-evaluation of the inside pass: a 64x64 contraction per internal child, the
+    children's products, the root dot."""
     return 8192 * (nl - 2) + 64 * (nl - 1) + 128
+
+
+def flops_per_column_grad(nl: int) -> int:
+    """Inside pass plus the adjoint: per branch a Q contraction and, for internal children, a
+    P^T contraction."""
+    return flops_per_column(nl) + 8192 * ((2 * nl - 2) + (nl - 2)) + 64 * 3 * (2 * nl - 2)
+
+
+def flops_per_column_tangent(nl: int) -> int:
+    """Forward-mode pass: three contractions per internal child (E alpha, E alpha', Q v), one per
+    leaf (Q v), the products of values and tangents."""
+    return 8192 * (3 * (nl - 2) + nl) + 64 * 4 * (nl - 1) + 256
+
+
+KERNEL_NAMES = {0: "k_prune (SIMT, {prec} returned values)", 1: "k_prune_tc<3> (tcgen05 search)",
+                2: "k_grad (adjoint)", 3: "k_prune_tc_dual (tcgen05 tangent)"}
+KERNEL_KEYS = {0: "simt_prune", 1: "tc_prune", 2: "grad", 3: "tc_tangent"}
 
 
 # ---------------------------------------------------------------- distributed
@@ -291,19 +310,30 @@ def run_ours(args, world, rank, local):
     e2e_value = world * wl.n_regions * args.steps / (ms_e2e / 1000.0)
     same = bool(np.array_equal(res_e2e["score"], res["score"]))
 
-    # roofline of the pruning kernel (FP32 SIMT path: CUDA-core FMA bound; reported against the
-    # measured tensor peak as the contract requires, with the FP32 FMA ceiling alongside)
+    # roofline of the dominant pruning kernel (by device time): algorithmic FLOPs of its launches
+    # (one product per contraction, whatever the split) over their device time.  The SIMT kernels
+    # are CUDA-core FMA bound; they are reported against the measured tensor peak as the contract
+    # requires, with the FP32 FMA ceiling alongside.
     peaks, peak_kind = load_peaks()
-    cols_evaluated = st["column_branches"] / nb
-    alg_flops = cols_evaluated * flops_per_column(nl)
-    prune_s = st["prune_ms"] / 1000.0
-    achieved_tflops = alg_flops / prune_s / 1e12 if prune_s > 0 else 0.0
+    kind = int(np.argmax(st["kind_ms"]))
+    kname = KERNEL_NAMES[kind].format(prec=args.precision)
+    kcols = st["kind_columns"][kind]
+    kflops = kcols * {0: flops_per_column, 1: flops_per_column, 2: flops_per_column_grad,
+                      3: flops_per_column_tangent}[kind](nl)
+    kms = st["kind_ms"][kind]
+    launches = max(st["kind_launches"][kind], 1)
+    achieved_tflops = kflops / (kms / 1000.0) / 1e12 if kms > 0 else 0.0
     peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
     sm_mhz = (clk or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-    launches = max(st["prune_launches"], 1)
-    traffic = load_traffic("prune_" + args.precision)
-    traffic_per_launch = (traffic * cols_evaluated / launches) if traffic else None
+    traffic = load_traffic(KERNEL_KEYS[kind])
+    traffic_per_launch = (traffic * kcols / launches) if traffic else None
+    shares = {KERNEL_KEYS[k]: st["kind_ms"][k] / args.steps for k in range(4)}
+    shares["pform"] = st["pform_ms"] / args.steps
+    kinds = {KERNEL_KEYS[k]: {"launches_per_step": st["kind_launches"][k] / args.steps,
+                              "column_evals_per_step": st["kind_columns"][k] / args.steps,
+                              "ns_per_column_eval": (1e6 * st["kind_ms"][k] / st["kind_columns"][k]
+                                                     if st["kind_columns"][k] else None)} for k in range(4)}
 
     line = {"metric": METRIC, "value": value, "unit": "regions/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -322,14 +352,14 @@ def run_ours(args, world, rank, local):
             "gpu_launches": int(st["kernel_launches"]),
             "rounds_per_step": st["rounds"] / args.steps,
             "evaluations_per_step": st["evaluations"] / args.steps,
-            "roofline": {"kernel": "k_prune<%s>" % args.precision, "bound": "tensor", "achieved": achieved_tflops,
+            "roofline": {"kernel": kname, "bound": "tensor", "achieved": achieved_tflops,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved_tflops / peak,
                          "peak_kind": peak_kind + " bf16 sustained",
-                         "traffic": traffic_per_launch, "alg_flops_per_launch": alg_flops / launches,
-                         "avg_launch_ms": st["prune_ms"] / launches,
+                         "traffic": traffic_per_launch, "alg_flops_per_launch": kflops / launches,
+                         "avg_launch_ms": kms / launches, "launches": int(launches),
                          "fp32_fma_peak_tflops": fp32_peak, "frac_of_fp32_fma_peak": achieved_tflops / fp32_peak},
-            "kernel_ms_per_step": {"prune": st["prune_ms"] / args.steps, "pform": st["pform_ms"] / args.steps,
-                                   "other": st["other_ms"] / args.steps},
+            "kernel_ms_per_step": dict(shares, other=st["other_ms"] / args.steps),
+            "pruning_kernels": kinds,
             "clocks": clk}
 
     if rank == 0 and not args.no_accuracy:

@@ -115,6 +115,11 @@ typedef struct {
     double other_ms;             /* device time of the other kernels            */
     int64_t prune_launches;
     int64_t pform_launches;
+    /* by pruning-kernel kind: 0 SIMT (returned values), 1 tensor core (search),
+     * 2 adjoint gradient, 3 tensor-core tangent (d lpr / d rho for the search) */
+    int64_t kind_launches[4];
+    int64_t kind_columns[4];     /* codon-column evaluations (columns x requests)  */
+    double kind_ms[4];           /* device time (these sum to prune_ms)            */
     int32_t prune_grid;     /* launch configuration (not counters): CTAs of the SIMT pruning kernel, */
     int32_t tc_grid;        /* and of the tensor-core kernel (0 if the engine has none)              */
 } pcsf_stats;
@@ -198,7 +203,10 @@ int pcsf_lpr(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, do
  * NULL) and d lpr / d rho (d_rho: [n_regions]).  The reference's
  * equivalent is PhyloEM.d_ell_dtree via branch posteriors (PhyloEM.ml:140-182,
  * PhyloLik.ml:96-174, Q.ml:260-275); it is the backward of pcsf_lpr in the
- * sense of an autograd.Function. */
+ * sense of an autograd.Function.  On a tensor-core engine created with
+ * PCSF_TC_DIRECT, d_branch == NULL selects the forward-mode tangent pass on the
+ * tensor cores (lpr and d lpr / d rho only), the derivative the engine's own
+ * rho search uses. */
 int pcsf_grad(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, double *lpr, double *d_branch,
               double *d_rho, int32_t *status);
 

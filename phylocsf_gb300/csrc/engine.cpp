@@ -118,11 +118,13 @@ struct pcsf_engine {
 
     // models (host copies)
     double U[2][K2], lam[2][K], sq[2][K], isq[2][K], wrow[2][K], prior[2][K], wlog[2][K];
+    int16_t wlist[2][WLIST];
     float Uf[2][K2];
     double tol = 1e-6;
 
     // device copies
     DevBuf<double> dU, dlam, dsq, disq, dwrow, dprior, dwlog, dbranch;
+    DevBuf<int16_t> dwlist;
     DevBuf<float> dUf, dgridT, dgrid_eg, dQf, dQ2f;
     DevBuf<double> dgrid_t;
     DevBuf<SchedNode> dsched;
@@ -133,6 +135,9 @@ struct pcsf_engine {
     DevBuf<double> Pbuf64;
     DevBuf<float> Bop;             // tensor-core B operands of the branches above internal nodes
     DevBuf<float> dPfB;            // B operand of the tensor-core P(t) formation, per model
+    DevBuf<float> dQop;            // B operand of Q for the tangent pass, per model
+    DevBuf<double> ddpart, ddrho, ddscr;
+    bool dual_ok = false;          // the tangent pass fits this tree
     int tc_grid = 0;
     size_t pbuf_psets = 0;
     DevBuf<PSet> dps;
@@ -365,6 +370,19 @@ static int build_pt_grid(pcsf_engine *e, const double *Q[2])
     return PCSF_OK;
 }
 
+// The eigen-directions with w_m != 0 (normally the stationary one alone), for
+// the row-sum check of the P(t) kernels; wl[0] = -2 when there are more than WLIST.
+static void make_wlist(const double *w, int16_t *wl)
+{
+    int k = 0;
+    for (int mm = 0; mm < K; mm++)
+        if (w[mm] != 0.0) {
+            if (k == WLIST) { wl[0] = -2; return; }
+            wl[k++] = (int16_t)mm;
+        }
+    for (; k < WLIST; k++) wl[k] = -1;
+}
+
 static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2], const double *prior[2])
 {
     // symmetric similarity transforms A = D^1/2 Q D^-1/2, eigendecomposed in FP64 on the device
@@ -415,7 +433,10 @@ static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2],
             e->wrow[m][mm] = (std::fabs(w) > 1e-9 * nrm) ? w : 0.0;
         }
         for (int i = 0; i < K2; i++) e->Uf[m][i] = (float)e->U[m][i];
+        make_wlist(e->wrow[m], e->wlist[m]);
     }
+    CK(e->dwlist.reserve(2 * WLIST), "cudaMalloc");
+    CK(cudaMemcpyAsync(e->dwlist.p, e->wlist, sizeof(int16_t) * 2 * WLIST, cudaMemcpyHostToDevice, e->stream), "H2D");
     CK(e->dU.reserve(2 * K2), "cudaMalloc");
     CK(e->dUf.reserve(2 * K2), "cudaMalloc");
     CK(e->dlam.reserve(2 * K), "cudaMalloc");
@@ -439,6 +460,7 @@ static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2],
     e->dm.sq = e->dsq.p;
     e->dm.isq = e->disq.p;
     e->dm.wrow = e->dwrow.p;
+    e->dm.wlist = e->dwlist.p;
     e->dm.prior = e->dprior.p;
     e->dm.wlog = e->dwlog.p;
     e->dm.tol = e->tol;
@@ -461,6 +483,24 @@ static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2],
                     bpf[o] = hi;
                     bpf[o + K2] = x - hi;
                 }
+        // B operand of Q for the tangent pass: B[a][j] = Q[a][j], same layout
+        std::vector<float> qop((size_t)2 * 2 * K2);
+        for (int m = 0; m < 2; m++)
+            for (int aa = 0; aa < K; aa++)
+                for (int j = 0; j < K; j++) {
+                    const float x = (float)Q[m][aa * K + j];
+                    uint32_t bits;
+                    std::memcpy(&bits, &x, 4);
+                    bits &= 0xFFFFE000u;
+                    float hi;
+                    std::memcpy(&hi, &bits, 4);
+                    const size_t o = (size_t)m * 2 * K2 + (j / 4) * 256 + aa * 4 + j % 4;
+                    qop[o] = hi;
+                    qop[o + K2] = x - hi;
+                }
+        CK(e->dQop.reserve(qop.size()), "cudaMalloc");
+        CK(cudaMemcpyAsync(e->dQop.p, qop.data(), sizeof(float) * qop.size(), cudaMemcpyHostToDevice, e->stream), "H2D");
+        e->dual_ok = prune_tc_dual_supported(e->nslots, e->nl);
         CK(e->dPfB.reserve(bpf.size()), "cudaMalloc");
         CK(cudaMemcpyAsync(e->dPfB.p, bpf.data(), sizeof(float) * bpf.size(), cudaMemcpyHostToDevice, e->stream), "H2D");
         CK(cudaStreamSynchronize(e->stream), "model upload");
@@ -567,7 +607,8 @@ struct Eval {
 // engine's two fixed models; their P(t) is formed in FP64 (no FP32 grid exists
 // for them) and the pruning runs on the SIMT kernels.
 static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &reqs_in, std::vector<Eval> &out,
-                    std::vector<double> *grad = nullptr, bool accurate = false, const DevModels *dyn = nullptr)
+                    std::vector<double> *grad = nullptr, bool accurate = false, const DevModels *dyn = nullptr,
+                    std::vector<double> *drho = nullptr)
 {
     const int nreq = (int)reqs_in.size();
     out.assign(nreq, Eval{0.0, 0.0, PCSF_OK});
@@ -575,12 +616,16 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     if (dyn && grad) return e->fail(PCSF_EINVAL, "gradients are not available for per-request models");
     if (dyn) accurate = true;
     const DevModels dmv = dyn ? *dyn : e->dm;
+    if (drho && (grad || dyn || accurate || !e->dual_ok))
+        return e->fail(PCSF_EINVAL, "d lpr / d rho by the tangent pass needs a tensor-core engine and a tree of <= 4 slots");
     const bool tc = (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32) && !accurate;
     // the gradient always runs the SIMT adjoint kernel (64-column tiles in FP32)
     const int TC = (grad || !tc) ? (e->prec == PCSF_PREC_FP64 ? 32 : 64) : prune_tile_cols(e->prec);
     const int comp = (accurate && (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32)) ? e->accurate_comp()
                                                                                               : e->comp_mode();
 
+    const int kind = drho ? 3 : grad ? 2 : tc ? 1 : 0;
+    int64_t kind_cols = 0;
     // work items, P-set dedup and chunking (at most pbuf_psets distinct P sets per chunk)
     std::vector<Request> reqs(reqs_in);
     std::vector<int> wib(nreq + 1, 0);
@@ -621,6 +666,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
             wis.push_back(w);
         }
         e->stats.column_branches += (c1 - c0) * (int64_t)e->nbr;
+        kind_cols += c1 - c0;
     }
     wib[nreq] = (int)wis.size();
     chunk_req_begin.push_back(nreq);
@@ -643,6 +689,11 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     CK(e->dpart.reserve(2 * (size_t)std::max(nwi, 1)), "cudaMalloc");
     CK(e->dlpr.reserve(nreq), "cudaMalloc");
     CK(e->delpr.reserve(nreq), "cudaMalloc");
+    if (drho) {
+        CK(e->ddpart.reserve(2 * (size_t)std::max(nwi, 1)), "cudaMalloc");
+        CK(e->ddrho.reserve(nreq), "cudaMalloc");
+        CK(e->ddscr.reserve(nreq), "cudaMalloc");
+    }
     size_t pset_bytes = (size_t)e->nbr * K2 * (e->prec == PCSF_PREC_FP64 ? 8 : 4);
     size_t max_chunk_ps = 0;
     for (size_t c = 0; c + 1 < chunk_ps_begin.size(); c++)
@@ -732,6 +783,10 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
             const bool tce = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
             CK(launch_grad(e->prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32,
                            tce ? e->accurate_comp() : e->comp_mode(), ga, s, grid), "gradient launch");
+        } else if (drho) {
+            int grid = std::min(e->sm_count, std::max(pa.nwi, 1));
+            CK(launch_prune_tc_dual(pa, e->dQop.p, e->dbranch.p, e->ddpart.p + 2 * (size_t)wib[r0], e->derr.p, s, grid),
+               "tensor-core tangent launch");
         } else if (tc) {
             int grid = std::min(e->tc_grid, std::max(pa.nwi, 1));
             CK(launch_prune_tc(e->prec == PCSF_PREC_TF32X3 ? 3 : 1, pa, e->derr.p, s, grid), "tensor-core pruning launch");
@@ -743,6 +798,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         CK(cudaEventRecord(e->ev[2], s), "event");
         e->stats.pform_launches += (p1 > p0);
         e->stats.prune_launches += (pa.nwi > 0);
+        e->stats.kind_launches[kind] += (pa.nwi > 0);
         e->stats.kernel_launches += (p1 > p0) + (pa.nwi > 0);
         CK(cudaEventSynchronize(e->ev[2]), "pruning");
         float t1 = 0.f, t2 = 0.f;
@@ -754,6 +810,13 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     CK(cudaEventRecord(e->ev[3], s), "event");
     CK(launch_reduce(e->dpart.p, e->dwib.p, nreq, e->dlpr.p, e->delpr.p, s), "reduce launch");
     e->stats.kernel_launches += 1;
+    std::vector<double> hdrho;
+    if (drho) {
+        CK(launch_reduce(e->ddpart.p, e->dwib.p, nreq, e->ddrho.p, e->ddscr.p, s), "reduce launch");
+        e->stats.kernel_launches += 1;
+        hdrho.resize(nreq);
+        CK(cudaMemcpyAsync(hdrho.data(), e->ddrho.p, sizeof(double) * nreq, cudaMemcpyDeviceToHost, s), "D2H drho");
+    }
     if (grad) {
         CK(launch_reduce_grad(e->dgpart.p, e->dwib.p, nreq, e->nbr, e->dgrad.p, s), "gradient reduce launch");
         e->stats.kernel_launches += 1;
@@ -771,6 +834,8 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     cudaEventElapsedTime(&rd_ms, e->ev[3], e->ev[4]);
     e->stats.pform_ms += pf_ms;
     e->stats.prune_ms += pr_ms;
+    e->stats.kind_ms[kind] += pr_ms;
+    e->stats.kind_columns[kind] += kind_cols;
     e->stats.other_ms += rd_ms;
     for (int r = 0; r < nreq; r++) {
         int key = e->hstatus.p[req_pset_global[r]];
@@ -778,6 +843,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         out[r] = Eval{e->hlpr.p[r], e->helpr.p[r], st};
     }
     if (grad) grad->assign(e->hgrad.p, e->hgrad.p + (size_t)nreq * e->nbr);
+    if (drho) *drho = hdrho;
     return PCSF_OK;
 }
 
@@ -1039,7 +1105,7 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
     std::vector<Request> reqs, greqs, areqs;
     std::vector<std::pair<int, double>> owner, gowner, aowner;
     std::vector<Eval> res, gres, ares;
-    std::vector<double> grad;
+    std::vector<double> grad, drho;
     for (;;) {
         reqs.clear();
         owner.clear();
@@ -1094,8 +1160,10 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
             int rc = evaluate(e, b, reqs, res);
             if (rc) return rc;
         }
+        const bool tangent = e->dual_ok && (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32);
         if (!greqs.empty()) {
-            int rc = evaluate(e, b, greqs, gres, &grad);
+            int rc = tangent ? evaluate(e, b, greqs, gres, nullptr, false, nullptr, &drho)
+                             : evaluate(e, b, greqs, gres, &grad);
             if (rc) return rc;
         }
         if (!areqs.empty()) {
@@ -1115,7 +1183,9 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
             Fit &f = fits[gowner[k].first];
             const double r = gowner[k].second;
             double dr = 0.0;
-            for (int c = 0; c < e->nbr; c++) dr += e->branch[c] * grad[k * e->nbr + c];
+            if (tangent) dr = drho[k];
+            else
+                for (int c = 0; c < e->nbr; c++) dr += e->branch[c] * grad[k * e->nbr + c];
             f.gcache.push_back({r, dr});
             if (!f.get(r)) f.cache.push_back({r, gres[k]});
             if (f.region == trace)
@@ -1266,6 +1336,7 @@ struct DynModels {
     std::map<OmegaKey, int> index;                  // key -> cache slot
     std::vector<std::vector<double>> U, lam, eq;    // host cache
     DevBuf<double> dU, dlam, dsq, disq, dwrow, dprior, dwlog;
+    DevBuf<int16_t> dwlist;
     DevBuf<float> dUf;
     DevModels dm{};
 };
@@ -1329,6 +1400,7 @@ static int dyn_prepare(pcsf_engine *e, DynModels &dmod, const std::vector<OmegaK
     std::vector<double> U((size_t)M * K2), lam((size_t)M * K), sq((size_t)M * K), isq((size_t)M * K),
         wrow((size_t)M * K), prior((size_t)M * K), wlog((size_t)M * K);
     std::vector<float> Uf((size_t)M * K2);
+    std::vector<int16_t> wlist((size_t)M * WLIST);
     for (int m = 0; m < M; m++) {
         const int id = slot[m];
         const std::vector<double> &eqv = dmod.eq[id];
@@ -1351,7 +1423,11 @@ static int dyn_prepare(pcsf_engine *e, DynModels &dmod, const std::vector<OmegaK
             for (int j = 0; j < K; j++) w += dmod.U[id][j * K + mm] * sq[(size_t)m * K + j];
             wrow[(size_t)m * K + mm] = (std::fabs(w) > 1e-9 * nrm) ? w : 0.0;
         }
+        make_wlist(&wrow[(size_t)m * K], &wlist[(size_t)m * WLIST]);
     }
+    CK(dmod.dwlist.reserve((size_t)M * WLIST), "cudaMalloc");
+    CK(cudaMemcpyAsync(dmod.dwlist.p, wlist.data(), sizeof(int16_t) * M * WLIST, cudaMemcpyHostToDevice, e->stream),
+       "H2D");
     CK(dmod.dU.reserve((size_t)M * K2), "cudaMalloc");
     CK(dmod.dUf.reserve((size_t)M * K2), "cudaMalloc");
     for (auto *bp : {&dmod.dlam, &dmod.dsq, &dmod.disq, &dmod.dwrow, &dmod.dprior, &dmod.dwlog})
@@ -1372,6 +1448,7 @@ static int dyn_prepare(pcsf_engine *e, DynModels &dmod, const std::vector<OmegaK
     dmod.dm.sq = dmod.dsq.p;
     dmod.dm.isq = dmod.disq.p;
     dmod.dm.wrow = dmod.dwrow.p;
+    dmod.dm.wlist = dmod.dwlist.p;
     dmod.dm.prior = dmod.dprior.p;
     dmod.dm.wlog = dmod.dwlog.p;
     dmod.dm.tol = e->tol;
@@ -1852,6 +1929,18 @@ int pcsf_grad(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, d
     }
     std::vector<Eval> res;
     std::vector<double> g;
+    if (!d_branch && e->tc_direct && e->dual_ok) {
+        // precision-study mode: lpr and d lpr / d rho straight from the tensor-core tangent pass
+        std::vector<double> dr;
+        int rc = evaluate(e, b, reqs, res, nullptr, false, nullptr, &dr);
+        if (rc) return rc;
+        for (int r = 0; r < b->nreg; r++) {
+            lpr[r] = res[r].lpr;
+            if (status) status[r] = res[r].status;
+            if (d_rho) d_rho[r] = dr[r];
+        }
+        return PCSF_OK;
+    }
     int rc = evaluate(e, b, reqs, res, &g);
     if (rc) return rc;
     for (int r = 0; r < b->nreg; r++) {

@@ -278,12 +278,7 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
         if (tid < K && !raw) {
             const int i = tid;
             // raw row sum - 1, in FP64 through the eigensystem
-            double rs = 0.0;
-            for (int mm = 0; mm < K; mm++) {
-                double w = wrow[mm];
-                if (w != 0.0) rs += U[i * K + mm] * ex[mm] * w;
-            }
-            rs *= isq[i];
+            const double rs = rowsum_minus_one(m, md, i, ex);
             // the diagonal is the compensated sum of the stored (rounded)
             // off-diagonal entries, so every stored row of P = I + E sums to 1
             // to within one rounding of the diagonal; a plain FP32 sum here

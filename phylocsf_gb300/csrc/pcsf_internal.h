@@ -44,6 +44,7 @@ struct WorkItem {
 };
 
 // Device view of the two models' eigensystems (all arrays [2][...]).
+constexpr int WLIST = 4;
 struct DevModels {
     const double *U;        // [2][K][K]  eigenvectors of D^1/2 Q D^-1/2 (columns)
     const float *Uf;        // [2][K][K]  FP32 copy
@@ -51,6 +52,7 @@ struct DevModels {
     const double *sq;       // [2][K]     sqrt(pi)
     const double *isq;      // [2][K]     1/sqrt(pi)
     const double *wrow;     // [2][K]     w_m = sum_j U_jm sqrt(pi_j)  (row-sum identity)
+    const int16_t *wlist;   // [2][WLIST] the m with w_m != 0, -1 padded; wlist[0] = -2: more than WLIST
     const double *prior;    // [2][K]     root prior
     const double *wlog;     // [2][K]     prior_a * log(prior_a)
     double tol;             // Q.Diag tol (1e-6)
@@ -147,6 +149,13 @@ int prune_tc_ctas_per_sm(int nslots, int nl, int nint);
 // nodes into Bop; Bpf = per model the pre-split B = U^T D^1/2 [2][hi, lo][64 x 64]
 cudaError_t launch_pform_tc(const PSet *ps, int nps, const double *branch, int nbr, int nl, DevModels m,
                             const float *Bpf, float *Pbuf, float *Bop, int32_t *status_key, int *err, cudaStream_t s);
+// tensor-core tangent pass (tc_dual.cu): lpr / elpr partials as k_prune_tc plus
+// d lpr / d rho partials dpart [nwi][2] (second entry 0); Qop = per model the
+// pre-split B operand of Q [2][hi, lo][64 x 64]; branch = the tree's lengths
+cudaError_t launch_prune_tc_dual(const PruneArgs &a, const float *Qop, const double *branch, double *dpart, int *err,
+                                 cudaStream_t s, int grid);
+size_t prune_tc_dual_smem_bytes(int nl, int nint);
+bool prune_tc_dual_supported(int nslots, int nl);
 
 // Sum the partials of each request's contiguous work items in fixed order.
 cudaError_t launch_reduce(const double *partials, const int32_t *wi_begin, int nreq, double *out_lpr,

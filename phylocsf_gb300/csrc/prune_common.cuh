@@ -77,6 +77,24 @@ __device__ __forceinline__ void bop_store(float *dst, int a, int q, float4 x)
     *reinterpret_cast<float4 *>(dst + K2 + q * 256 + a * 4) = l;
 }
 
+// Row sum of the raw P(t) minus one, through the eigensystem: isq_i sum_m U_im
+// expm1(lam_m t) w_m, where only the stationary direction(s) have w_m != 0;
+// ex[m] = expm1(lam_m t) must be valid for those m.
+__device__ __forceinline__ double rowsum_minus_one(const DevModels &m, int md, int i, const double *ex)
+{
+    const double *U = m.U + (size_t)md * K2 + (size_t)i * K;
+    const double *w = m.wrow + md * K;
+    const int16_t *wl = m.wlist + md * WLIST;
+    double rs = 0.0;
+    if (wl[0] == -2) {
+        for (int mm = 0; mm < K; mm++)
+            if (w[mm] != 0.0) rs += U[mm] * ex[mm] * w[mm];
+    } else {
+        for (int k = 0; k < WLIST && wl[k] >= 0; k++) rs += U[wl[k]] * ex[wl[k]] * w[wl[k]];
+    }
+    return rs * m.isq[md * K + i];
+}
+
 // exp_of(x): the e of frexp (x = m 2^e, m in [0.5, 1)) read from the exponent
 // field for normal x; frexp itself for zero, subnormals and non-finite x.
 __device__ __forceinline__ int exp_of(float x)

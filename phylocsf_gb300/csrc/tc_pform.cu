@@ -34,6 +34,7 @@ constexpr uint32_t PFT_B = 0;          // [hi, lo][64 x 64]   B = U^T D^1/2, 2 x
 constexpr uint32_t PFT_A = 32768;      // [hi, lo][128 x 64]  A, 2 x 32 KB
 constexpr uint32_t PFT_SMEM = 98304;
 constexpr uint32_t PFT_TMEM_COLS = 64;
+constexpr int PFT_MAX_BRANCHES = 320;
 
 __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const double *branch, int nbr, int nl,
                                                           DevModels m, const float *Bpf, float *Pbuf, float *Bop,
@@ -43,9 +44,9 @@ __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const 
     __shared__ uint32_t tbase_s;
     __shared__ __align__(8) uint64_t bar_mma, bar_b;
     __shared__ float cfs[2][K];
-    __shared__ double exs[2][K];        // expm1(lam t) where w_m != 0 (row-sum check)
-    __shared__ int mode_s[2], g_s[2];
-    __shared__ double t_s[2];
+    __shared__ double exs[2][K];        // expm1(lam_m t) where w_m != 0 (row-sum check)
+    __shared__ int mode_g[PFT_MAX_BRANCHES];      // per branch: grid point << 2 | mode
+    __shared__ double t_b[PFT_MAX_BRANCHES];
 
     const int tid = threadIdx.x;
     const int r = blockIdx.x;           // P set (chunk-local)
@@ -82,41 +83,37 @@ __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const 
     uint32_t ph = 0;
     bool pending = false;               // an MMA group was issued and its completion not seen
     const float isq_i = (float)m.isq[md * K + i];
+    // per branch: 0 t = 0, 1 below the grid (Taylor), 2 grid correction at point g
+    for (int b = tid; b < nbr; b += PFT_THREADS) {
+        const double t = rq.rho * branch[b];
+        int mode = 0, g = 0;
+        if (t == 0.0) mode = 0;
+        else if (t < m.grid_t[0]) mode = 1;
+        else {
+            mode = 2;
+            const double x = log(t / m.grid_t[0]) / m.grid_lr;
+            g = (int)floor(x);
+            if (g < 0) g = 0;
+            if (g > m.grid_n - 1) g = m.grid_n - 1;
+            if (g + 1 < m.grid_n && (m.grid_t[g + 1] - t) < (t - m.grid_t[g])) g++;
+        }
+        mode_g[b] = (g << 2) | mode;
+        t_b[b] = t;
+    }
 
     for (int b0 = 0; b0 < nbr; b0 += 2) {
-        // ---- per-branch mode, grid point, coefficients
-        if (tid < 2) {
-            const int b = b0 + tid;
-            int mode = 1, g = 0;
-            double t = 0.0;
-            if (b < nbr) {
-                t = rq.rho * branch[b];
-                if (t == 0.0) mode = 1;
-                else if (t < m.grid_t[0]) mode = 2;
-                else {
-                    mode = 3;
-                    const double x = log(t / m.grid_t[0]) / m.grid_lr;
-                    g = (int)floor(x);
-                    if (g < 0) g = 0;
-                    if (g > m.grid_n - 1) g = m.grid_n - 1;
-                    if (g + 1 < m.grid_n && (m.grid_t[g + 1] - t) < (t - m.grid_t[g])) g++;
-                }
-            }
-            mode_s[tid] = mode;
-            g_s[tid] = g;
-            t_s[tid] = t;
-            for (int mm = 0; mm < K; mm++) exs[tid][mm] = (wrow[mm] != 0.0) ? expm1(lam[mm] * t) : 0.0;
-        }
-        if (__syncthreads_or(!ok)) break;
+        const int b = b0 + bsel;                      // this thread's branch
+        if (__syncthreads_or(!ok)) break;             // per-branch table ready / previous pair done
+        const int mode = (b < nbr) ? (mode_g[b] & 3) : 0, g = (b < nbr) ? (mode_g[b] >> 2) : 0;
+        const double t = (b < nbr) ? t_b[b] : 0.0;
         {
-            const int mode = mode_s[bsel];
             float cf = 0.0f;
-            if (mode == 3) {
-                const int g = g_s[bsel];
-                const double h = t_s[bsel] - m.grid_t[g];
+            if (mode == 2) {
+                const double h = t - m.grid_t[g];
                 cf = m.grid_eg[((size_t)md * m.grid_n + g) * K + i] * expm1f((float)(lam[i] * h));
             }
             cfs[bsel][i] = cf;      // thread (bsel, i) supplies coefficient m = i
+            exs[bsel][i] = (wrow[i] != 0.0) ? expm1(lam[i] * t) : 0.0;
         }
         __syncthreads();
         // ---- A operand: row tid = isq_i U_im cf_m, TF32 hi / lo
@@ -150,30 +147,31 @@ __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const 
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                          :: "r"(barM) : "memory");
         }
+        // ---- epilogue inputs that do not depend on D, loaded while the MMAs run
+        float row[K];
+        {
+            const float *eg = m.gridT + ((size_t)md * m.grid_n + g) * K2;   // E(t_g)^T
+            const float *Qf = m.Qf + (size_t)md * K2 + (size_t)i * K, *Q2f = m.Q2f + (size_t)md * K2 + (size_t)i * K;
+            const float tt = (float)t, h2 = (float)(0.5 * t * t);
+#pragma unroll
+            for (int j = 0; j < K; j++) {
+                if (mode == 2) row[j] = __ldg(eg + (size_t)j * K + i);
+                else if (mode == 1) row[j] = tt * Qf[j] + h2 * Q2f[j];
+                else row[j] = 0.0f;
+            }
+        }
         pending = true;
         const bool done = mbar_wait(barM, ph);
         ph ^= 1u;
         if (done) pending = false;
         tc_fence_after();
-        // ---- epilogue: row i of branch b
-        const int b = b0 + bsel;
-        const int mode = mode_s[bsel];
-        const float *eg = m.gridT + ((size_t)md * m.grid_n + g_s[bsel]) * K2;   // E(t_g)^T
-        const float *Qf = m.Qf + (size_t)md * K2 + (size_t)i * K, *Q2f = m.Q2f + (size_t)md * K2 + (size_t)i * K;
-        const float tt = (float)t_s[bsel], h2 = (float)(0.5 * t_s[bsel] * t_s[bsel]);
-        float row[K];
+        if (mode == 2) {
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-            float d[16];
-            tmem_ld16(tbase + lane_off + 16 * c, d);
+            for (int c = 0; c < 4; c++) {
+                float d[16];
+                tmem_ld16(tbase + lane_off + 16 * c, d);
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-                const int jj = 16 * c + j;
-                float x;
-                if (mode == 3) x = d[j] + __ldg(eg + (size_t)jj * K + i);
-                else if (mode == 2) x = tt * Qf[jj] + h2 * Q2f[jj];
-                else x = 0.0f;
-                row[jj] = x;
+                for (int j = 0; j < 16; j++) row[16 * c + j] += d[j];
             }
         }
         tc_fence_before();
@@ -200,12 +198,7 @@ __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const 
 #pragma unroll
             for (int j = 0; j < K; j++)
                 if (j == i) row[j] = diag;
-            double rs = 0.0;
-            for (int mm = 0; mm < K; mm++) {
-                const double w = wrow[mm];
-                if (w != 0.0) rs += m.U[(size_t)md * K2 + i * K + mm] * exs[bsel][mm] * w;
-            }
-            rs *= m.isq[md * K + i];
+            const double rs = rowsum_minus_one(m, md, i, exs[bsel]);
             if (neg) status_min(status_key + r, b, i, PCSF_ENEGP);
             else if (fabs(rs) > m.tol) status_min(status_key + r, b, i, PCSF_EROWSUM);
             else if (!((double)diag > -1.0)) status_min(status_key + r, b, i, PCSF_EDIAG);
@@ -220,9 +213,10 @@ __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const 
                 for (int j = 0; j < K; j++) out[(size_t)j * K + i] = row[j];
             }
         }
-        if (__syncthreads_or(!done)) { ok = false; break; }    // D is read: the next pair may overwrite it
+        if (!done) ok = false;      // agreed on at the next pair's first barrier
         tc_fence_after();
     }
+    if (__syncthreads_or(!ok)) ok = false;
     if (!ok && tid == 0) atomicExch(err, 1);
     if (pending) mbar_wait(barM, ph ^ 1u);
     tc_fence_before();

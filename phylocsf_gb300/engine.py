@@ -78,6 +78,8 @@ class Stats(ctypes.Structure):
                 ("column_branches", ctypes.c_int64), ("rounds", ctypes.c_int64),
                 ("prune_ms", ctypes.c_double), ("pform_ms", ctypes.c_double), ("other_ms", ctypes.c_double),
                 ("prune_launches", ctypes.c_int64), ("pform_launches", ctypes.c_int64),
+                ("kind_launches", ctypes.c_int64 * 4), ("kind_columns", ctypes.c_int64 * 4),
+                ("kind_ms", ctypes.c_double * 4),
                 ("prune_grid", ctypes.c_int32), ("tc_grid", ctypes.c_int32)]
 
 
@@ -377,16 +379,18 @@ class Engine:
                self.handle)
         return lpr, elpr, st
 
-    def grad(self, batch: Batch, model: int, rho):
+    def grad(self, batch: Batch, model: int, rho, branches: bool = True):
+        """(lpr, d lpr / d branch or None, d lpr / d rho, status).  branches=False asks for
+        d lpr / d rho alone (on a *_direct tensor-core engine: by the tangent pass)."""
         r = np.ascontiguousarray(np.broadcast_to(np.asarray(rho, np.float64), (batch.n_regions,)))
         nbr = self.tree.n - 1
         lpr = np.zeros(batch.n_regions)
-        db = np.zeros((batch.n_regions, nbr))
+        db = np.zeros((batch.n_regions, nbr)) if branches else None
         drho = np.zeros(batch.n_regions)
         st = np.zeros(batch.n_regions, np.int32)
         _check(self.lib.pcsf_grad(self.handle, batch.handle, model, _p(r, ctypes.c_double), _p(lpr, ctypes.c_double),
-                                  _p(db, ctypes.c_double), _p(drho, ctypes.c_double), _p(st, ctypes.c_int32)),
-               self.handle)
+                                  _p(db, ctypes.c_double) if branches else None, _p(drho, ctypes.c_double),
+                                  _p(st, ctypes.c_int32)), self.handle)
         return lpr, db, drho, st
 
     # ---- model introspection
@@ -408,7 +412,11 @@ class Engine:
     def stats(self) -> dict:
         s = Stats()
         _check(self.lib.pcsf_engine_get_stats(self.handle, ctypes.byref(s)), self.handle)
-        return {k: getattr(s, k) for k, _ in Stats._fields_}
+        out = {}
+        for k, _ in Stats._fields_:
+            v = getattr(s, k)
+            out[k] = list(v) if not isinstance(v, (int, float)) else v
+        return out
 
     def stream_handle(self) -> int:
         """The engine's cudaStream_t as an integer (for event timing on that stream)."""
