@@ -253,6 +253,20 @@ typedef struct {
  * reference defaults are omega_h1 = 0.2, sigma_h1 = 0.01. */
 int pcsf_omega_score(pcsf_engine *e, pcsf_batch *b, double omega_h1, double sigma_h1, pcsf_omega_result *out);
 
+/* Gradient of the OmegaModel log-likelihood (priors excluded) of every region
+ * at its own kappa[r], omega[r], the common sigma, the F3x4 frequencies of the
+ * region's leaves (update_f3x4, OmegaModel.ml:102-134) and tree scale rho[r]:
+ * lpr, d lpr / d branch ([n_regions][2*n_leaves-2], may be NULL), d / d rho,
+ * d / d kappa, d / d omega (each may be NULL).  The rate-parameter derivatives
+ * contract the adjoint pass's weights with dP(t)/dx, the eigenbasis (Frechet)
+ * derivative of exp(tQ) -- Q.Diag.dPt_dQ_dx, Q.ml:283-304 -- taken in the
+ * symmetric form D^1/2 Q D^-1/2 of the reversible Q; P(t) and Q are formed in
+ * FP64, the adjoint runs in the engine's precision.  Replaces the derivative
+ * the reference's PhyloEM.d_ell_dQ_dx computes (PhyloEM.ml:76-138). */
+int pcsf_omega_grad(pcsf_engine *e, pcsf_batch *b, const double *kappa, const double *omega, double sigma,
+                    const double *rho, double *lpr, double *d_branch, double *d_rho, double *d_kappa, double *d_omega,
+                    int32_t *status);
+
 #ifdef __cplusplus
 }
 #endif

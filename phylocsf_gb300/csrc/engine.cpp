@@ -17,6 +17,7 @@
 // performs and which give bit-identical results) are not recomputed.
 #include <algorithm>
 #include <array>
+#include <thread>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -136,6 +137,8 @@ struct pcsf_engine {
     DevBuf<float> Bop;             // tensor-core B operands of the branches above internal nodes
     DevBuf<float> dPfB;            // B operand of the tensor-core P(t) formation, per model
     DevBuf<float> dQop;            // B operand of Q for the tangent pass, per model
+    DevBuf<unsigned char> dHmat;   // parameter-derivative matrices per chunk-local P set
+    size_t smem_optin = 0;
     DevBuf<double> ddpart, ddrho, ddscr;
     bool dual_ok = false;          // the tangent pass fits this tree
     int tc_grid = 0;
@@ -560,6 +563,7 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
     CK(cudaMemcpyAsync(e->dsched.p, e->sched.data(), sizeof(SchedNode) * e->sched.size(), cudaMemcpyHostToDevice,
                        e->stream), "H2D");
     e->sm_count = prop.multiProcessorCount;
+    e->smem_optin = prop.sharedMemPerBlockOptin;
     CK(e->derr.reserve(1), "cudaMalloc");
     CK(cudaMemsetAsync(e->derr.p, 0, sizeof(int), e->stream), "memset");
     const bool tc = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
@@ -577,7 +581,7 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
     int per_sm = std::max(1, (int)(prop.sharedMemPerMultiprocessor / (smem + 1024)));
     per_sm = std::min(per_sm, 8);
     e->prune_grid = prop.multiProcessorCount * per_sm;
-    size_t gsmem = grad_smem_bytes(e->prec, e->nslots, e->nl, (int)e->sched.size());
+    size_t gsmem = grad_smem_bytes(e->prec, e->nslots, e->nl, (int)e->sched.size(), 0);
     if (gsmem > (size_t)prop.sharedMemPerBlockOptin)
         return e->fail(PCSF_EINVAL, "tree needs %zu B shared memory for the gradient", gsmem);
     int gper = std::max(1, std::min(4, (int)(prop.sharedMemPerMultiprocessor / (gsmem + 1024))));
@@ -606,14 +610,23 @@ struct Eval {
 // dyn: per-request models (Request.model indexes this table) instead of the
 // engine's two fixed models; their P(t) is formed in FP64 (no FP32 grid exists
 // for them) and the pruning runs on the SIMT kernels.
+// Rate-matrix parameter derivatives for per-request models (OmegaModel kappa, omega):
+// per model Q row-major, U, and Bdot_x = U^T D^1/2 (dQ/dx) D^-1/2 U, in the engine's
+// arithmetic type.
+struct DynGrad {
+    const void *Qrow, *Umat, *Bdot;
+};
+
 static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &reqs_in, std::vector<Eval> &out,
                     std::vector<double> *grad = nullptr, bool accurate = false, const DevModels *dyn = nullptr,
-                    std::vector<double> *drho = nullptr)
+                    std::vector<double> *drho = nullptr, const DynGrad *dg = nullptr)
 {
     const int nreq = (int)reqs_in.size();
     out.assign(nreq, Eval{0.0, 0.0, PCSF_OK});
     if (nreq == 0) return PCSF_OK;
-    if (dyn && grad) return e->fail(PCSF_EINVAL, "gradients are not available for per-request models");
+    if (dyn && grad && !dg) return e->fail(PCSF_EINVAL, "gradients for per-request models need their derivatives");
+    const int npar = (grad && dg) ? 2 : 0;
+    const int gstride = e->nbr + npar;
     if (dyn) accurate = true;
     const DevModels dmv = dyn ? *dyn : e->dm;
     if (drho && (grad || dyn || accurate || !e->dual_ok))
@@ -657,6 +670,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         }
         req_pset_global[r] = chunk_ps_begin.back() + q.pset;
         int64_t c0 = b->offs[q.region], c1 = b->offs[q.region + 1];
+        q.start = (uint32_t)c0;
         wib[r] = (int)wis.size();
         for (int64_t c = c0; c < c1; c += TC) {
             WorkItem w;
@@ -707,11 +721,16 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     float *bop = want_bop ? e->Bop.p : nullptr;
     size_t gscr = 0;
     if (grad) {
-        gscr = grad_scratch_per_cta(e->prec, e->nl);
+        gscr = grad_scratch_per_cta(e->prec, e->nl, npar);
         CK(e->gscratch.reserve(gscr * (size_t)e->grad_grid), "cudaMalloc gradient scratch");
-        CK(e->dgpart.reserve((size_t)std::max(nwi, 1) * e->nbr), "cudaMalloc");
-        CK(e->dgrad.reserve((size_t)nreq * e->nbr), "cudaMalloc");
-        CK(e->hgrad.reserve((size_t)nreq * e->nbr), "cudaMallocHost");
+        CK(e->dgpart.reserve((size_t)std::max(nwi, 1) * gstride), "cudaMalloc");
+        CK(e->dgrad.reserve((size_t)nreq * gstride), "cudaMalloc");
+        CK(e->hgrad.reserve((size_t)nreq * gstride), "cudaMallocHost");
+        if (npar)
+            CK(e->dHmat.reserve(max_chunk_ps * (size_t)e->nbr * npar * K2 * (e->prec == PCSF_PREC_FP64 ? 8 : 4)),
+               "cudaMalloc derivative matrices");
+        if (npar && grad_smem_bytes(e->prec, e->nslots, e->nl, (int)e->sched.size(), npar) > e->smem_optin)
+            return e->fail(PCSF_EINVAL, "parameter derivatives need more shared memory than this device has for this tree");
     }
 
     std::memcpy(e->hps.p, psets.data(), sizeof(PSet) * nps);
@@ -761,6 +780,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         pa.partials = e->dpart.p + 2 * (size_t)wib[r0];
         pa.Bop = bop;
         pa.nbop = nbop;
+        pa.dither = e->prec != PCSF_PREC_FP64;
         if (grad) {
             GradArgs ga{};
             ga.wi = pa.wi;
@@ -774,11 +794,17 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
             ga.nbr = pa.nbr;
             ga.nslots = pa.nslots;
             ga.m = pa.m;
-            ga.Qrow = e->prec == PCSF_PREC_FP64 ? (const void *)e->dQrowd.p : (const void *)e->dQrowf.p;
+            ga.Qrow = dg ? dg->Qrow : e->prec == PCSF_PREC_FP64 ? (const void *)e->dQrowd.p : (const void *)e->dQrowf.p;
+            ga.npar = npar;
+            ga.Umat = dg ? dg->Umat : nullptr;
+            ga.Hmat = e->dHmat.p;
+            if (npar)
+                CK(launch_hform(e->prec == PCSF_PREC_FP64, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, dmv.lam, dg->Bdot,
+                                e->dHmat.p, s), "derivative matrix launch");
             ga.scratch = e->gscratch.p;
             ga.scratch_per_cta = gscr;
             ga.partials = pa.partials;
-            ga.gpart = e->dgpart.p + (size_t)wib[r0] * e->nbr;
+            ga.gpart = e->dgpart.p + (size_t)wib[r0] * gstride;
             int grid = std::min(e->grad_grid, std::max(pa.nwi, 1));
             const bool tce = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
             CK(launch_grad(e->prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32,
@@ -818,9 +844,9 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         CK(cudaMemcpyAsync(hdrho.data(), e->ddrho.p, sizeof(double) * nreq, cudaMemcpyDeviceToHost, s), "D2H drho");
     }
     if (grad) {
-        CK(launch_reduce_grad(e->dgpart.p, e->dwib.p, nreq, e->nbr, e->dgrad.p, s), "gradient reduce launch");
+        CK(launch_reduce_grad(e->dgpart.p, e->dwib.p, nreq, gstride, e->dgrad.p, s), "gradient reduce launch");
         e->stats.kernel_launches += 1;
-        CK(cudaMemcpyAsync(e->hgrad.p, e->dgrad.p, sizeof(double) * nreq * e->nbr, cudaMemcpyDeviceToHost, s), "D2H grad");
+        CK(cudaMemcpyAsync(e->hgrad.p, e->dgrad.p, sizeof(double) * nreq * gstride, cudaMemcpyDeviceToHost, s), "D2H grad");
     }
     CK(cudaEventRecord(e->ev[4], s), "event");
     CK(cudaMemcpyAsync(e->hlpr.p, e->dlpr.p, sizeof(double) * nreq, cudaMemcpyDeviceToHost, s), "D2H lpr");
@@ -842,7 +868,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         int st = (key >= 0 && key < 0x7f000000) ? (key & 15) : PCSF_OK;
         out[r] = Eval{e->hlpr.p[r], e->helpr.p[r], st};
     }
-    if (grad) grad->assign(e->hgrad.p, e->hgrad.p + (size_t)nreq * e->nbr);
+    if (grad) grad->assign(e->hgrad.p, e->hgrad.p + (size_t)nreq * gstride);
     if (drho) *drho = hdrho;
     return PCSF_OK;
 }
@@ -1312,6 +1338,49 @@ static void omega_q(const OmegaKey &q, double *Q, double *pi)
     for (int i = 0; i < K2; i++) Q[i] = Q[i] / scale;
 }
 
+// dQ/dx of the scaled OmegaModel rate matrix for x = kappa (0) or omega (1): with
+// R the unscaled matrix (R_ij = pi_j kappa^[transition] omega^[nonsynonymous]) and
+// s = -sum_i pi_i R_ii, Q = R / s and dQ/dx = R'/s - R s'/s^2 (pi does not depend on
+// kappa or omega).
+static void omega_dq(const OmegaKey &q, int x, double *dQ)
+{
+    std::vector<double> Q(K2), pi(K), R(K2), dR(K2);
+    omega_q(q, Q.data(), pi.data());
+    static const char *aa = "KNKNTTTTRSRSIIMIQHQHPPPPRRRRLLLLEDEDAAAAGGGGVVVV*Y*YSSSS*CWCLFLF";
+    auto nuc = [](int i, int pos) { return pos == 0 ? i / 16 : pos == 1 ? (i / 4) % 4 : i % 4; };
+    auto is_stop = [](int i) { return i == 48 || i == 50 || i == 56; };
+    for (int i = 0; i < K; i++) {
+        double tot = 0.0, dtot = 0.0;
+        for (int j = 0; j < K; j++) {
+            double v = 0.0, dv = 0.0;
+            if (i != j) {
+                int nd = 0, a = 0, bb = 0;
+                for (int pos = 0; pos < 3; pos++)
+                    if (nuc(i, pos) != nuc(j, pos)) { nd++; a = nuc(i, pos); bb = nuc(j, pos); }
+                if (nd == 1) {
+                    const bool transition = (a + bb == 2 && a != 1 && bb != 1) || (a + bb == 4 && a != 2 && bb != 2);
+                    const bool nonsyn = !is_stop(i) && !is_stop(j) && aa[i] != aa[j];
+                    v = pi[j] * ((transition ? q[0] : 1.0) * (nonsyn ? q[1] : 1.0));
+                    if (x == 0 && transition) dv = v / q[0];
+                    if (x == 1 && nonsyn) dv = v / q[1];
+                }
+            }
+            R[i * K + j] = v;
+            dR[i * K + j] = dv;
+            tot += v;
+            dtot += dv;
+        }
+        R[i * K + i] = -tot;
+        dR[i * K + i] = -dtot;
+    }
+    double sc = 0.0, dsc = 0.0;
+    for (int i = 0; i < K; i++) {
+        sc -= pi[i] * R[i * K + i];
+        dsc -= pi[i] * dR[i * K + i];
+    }
+    for (int i = 0; i < K2; i++) dQ[i] = dR[i] / sc - R[i] * dsc / (sc * sc);
+}
+
 // half_cauchy_lpdf ~mode:1 ~scale:0.5 (OmegaModel.ml:148-156) and the Gamma(7, 0.25)
 // density of kappa - 1 (OmegaModel.ml:157; GSL gamma_pdf with shape a, scale b).
 static double prior_value(int kind, double x)
@@ -1339,6 +1408,7 @@ struct DynModels {
     DevBuf<int16_t> dwlist;
     DevBuf<float> dUf;
     DevModels dm{};
+    DevBuf<unsigned char> dQrow, dBdot;             // parameter derivatives (dyn_derivs)
 };
 
 static int dyn_prepare(pcsf_engine *e, DynModels &dmod, const std::vector<OmegaKey> &keys, std::vector<int> &slot)
@@ -1456,6 +1526,66 @@ static int dyn_prepare(pcsf_engine *e, DynModels &dmod, const std::vector<OmegaK
     return PCSF_OK;
 }
 
+// For the round's models (as laid out by dyn_prepare): Q row-major and
+// Bdot_x = U^T D^1/2 (dQ/dx) D^-1/2 U for x = kappa, omega, in the engine's
+// arithmetic type, on the device; dg points at them and at the round's U.
+static int dyn_derivs(pcsf_engine *e, DynModels &dmod, const std::vector<OmegaKey> &keys, const std::vector<int> &slot,
+                      DynGrad &dg)
+{
+    const int M = (int)keys.size();
+    const bool fp64 = e->prec == PCSF_PREC_FP64;
+    std::vector<double> Qall((size_t)M * K2), Ball((size_t)M * 2 * K2);
+    auto work = [&](int m0, int m1) {
+        std::vector<double> Q(K2), pi(K), dQ(K2), A(K2), T1(K2);
+        for (int m = m0; m < m1; m++) {
+            omega_q(keys[m], Q.data(), pi.data());
+            std::copy(Q.begin(), Q.end(), Qall.begin() + (size_t)m * K2);
+            const std::vector<double> &U = dmod.U[slot[m]];
+            const std::vector<double> &eq = dmod.eq[slot[m]];
+            for (int x = 0; x < 2; x++) {
+                omega_dq(keys[m], x, dQ.data());
+                for (int i = 0; i < K; i++)
+                    for (int j = 0; j < K; j++) A[i * K + j] = std::sqrt(eq[i]) * dQ[i * K + j] / std::sqrt(eq[j]);
+                // T1 = A U, Bdot = U^T T1
+                for (int i = 0; i < K; i++)
+                    for (int j = 0; j < K; j++) {
+                        double acc = 0.0;
+                        for (int k = 0; k < K; k++) acc += A[i * K + k] * U[k * K + j];
+                        T1[i * K + j] = acc;
+                    }
+                double *Bd = &Ball[((size_t)m * 2 + x) * K2];
+                for (int i = 0; i < K; i++)
+                    for (int j = 0; j < K; j++) {
+                        double acc = 0.0;
+                        for (int k = 0; k < K; k++) acc += U[k * K + i] * T1[k * K + j];
+                        Bd[i * K + j] = acc;
+                    }
+            }
+        }
+    };
+    const int nth = std::max(1, std::min<int>(16, (int)std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (int t = 0; t < nth; t++) th.emplace_back(work, (int)((int64_t)M * t / nth), (int)((int64_t)M * (t + 1) / nth));
+    for (auto &t : th) t.join();
+    const size_t es = fp64 ? 8 : 4;
+    CK(dmod.dQrow.reserve((size_t)M * K2 * es), "cudaMalloc");
+    CK(dmod.dBdot.reserve((size_t)M * 2 * K2 * es), "cudaMalloc");
+    if (fp64) {
+        CK(cudaMemcpyAsync(dmod.dQrow.p, Qall.data(), sizeof(double) * Qall.size(), cudaMemcpyHostToDevice, e->stream), "H2D");
+        CK(cudaMemcpyAsync(dmod.dBdot.p, Ball.data(), sizeof(double) * Ball.size(), cudaMemcpyHostToDevice, e->stream), "H2D");
+        CK(cudaStreamSynchronize(e->stream), "derivative upload");
+    } else {
+        std::vector<float> qf(Qall.begin(), Qall.end()), bf(Ball.begin(), Ball.end());
+        CK(cudaMemcpyAsync(dmod.dQrow.p, qf.data(), sizeof(float) * qf.size(), cudaMemcpyHostToDevice, e->stream), "H2D");
+        CK(cudaMemcpyAsync(dmod.dBdot.p, bf.data(), sizeof(float) * bf.size(), cudaMemcpyHostToDevice, e->stream), "H2D");
+        CK(cudaStreamSynchronize(e->stream), "derivative upload");
+    }
+    dg.Qrow = dmod.dQrow.p;
+    dg.Bdot = dmod.dBdot.p;
+    dg.Umat = fp64 ? (const void *)dmod.dm.U : (const void *)dmod.dm.Uf;
+    return PCSF_OK;
+}
+
 struct OmegaRegion {
     int region = 0;
     int64_t ncols = 0;
@@ -1487,6 +1617,30 @@ struct OmegaRegion {
     }
 };
 
+// update_f3x4 (OmegaModel.ml:102-134): per region and codon position, nucleotide
+// counts over the leaves (pseudocount 1), relative to T
+static int region_f3x4(pcsf_engine *e, pcsf_batch *b, std::vector<std::array<double, 9>> &out)
+{
+    out.assign(b->nreg, {});
+    std::vector<uint8_t> lv((size_t)b->total_cols * e->nl);
+    if (!lv.empty()) CK(cudaMemcpy(lv.data(), b->dleaves.p, lv.size(), cudaMemcpyDeviceToHost), "D2H leaves");
+    for (int r = 0; r < b->nreg; r++) {
+        double counts[3][4];
+        for (auto &row : counts)
+            for (double &c : row) c = 1.0;
+        for (size_t i = (size_t)b->offs[r] * e->nl; i < (size_t)b->offs[r + 1] * e->nl; i++) {
+            const int c = lv[i];
+            if (c >= K) continue;
+            counts[0][c / 16] += 1.0;
+            counts[1][(c / 4) % 4] += 1.0;
+            counts[2][c % 4] += 1.0;
+        }
+        for (int pos = 0; pos < 3; pos++)
+            for (int n = 0; n < 3; n++) out[r][3 * pos + n] = counts[pos][n] / counts[pos][3];
+    }
+    return PCSF_OK;
+}
+
 static int omega_impl(pcsf_engine *e, pcsf_batch *b, double omega_h1, double sigma_h1, pcsf_omega_result *out)
 {
     const int nreg = b->nreg;
@@ -1501,25 +1655,12 @@ static int omega_impl(pcsf_engine *e, pcsf_batch *b, double omega_h1, double sig
         R.q[2] = 1.0;
         R.start_fit();
     }
-    // F3x4 counts need the leaves on the host
     {
-        std::vector<uint8_t> lv((size_t)b->total_cols * e->nl);
-        if (!lv.empty())
-            CK(cudaMemcpy(lv.data(), b->dleaves.p, lv.size(), cudaMemcpyDeviceToHost), "D2H leaves");
-        for (int r = 0; r < nreg; r++) {
-            double counts[3][4];
-            for (auto &row : counts)
-                for (double &c : row) c = 1.0;
-            for (size_t i = (size_t)b->offs[r] * e->nl; i < (size_t)b->offs[r + 1] * e->nl; i++) {
-                const int c = lv[i];
-                if (c >= K) continue;
-                counts[0][c / 16] += 1.0;
-                counts[1][(c / 4) % 4] += 1.0;
-                counts[2][c % 4] += 1.0;
-            }
-            for (int pos = 0; pos < 3; pos++)
-                for (int n = 0; n < 3; n++) regs[r].q[3 + 3 * pos + n] = counts[pos][n] / counts[pos][3];
-        }
+        std::vector<std::array<double, 9>> f;
+        int rc = region_f3x4(e, b, f);
+        if (rc) return rc;
+        for (int r = 0; r < nreg; r++)
+            for (int k = 0; k < 9; k++) regs[r].q[3 + k] = f[r][k];
     }
     DynModels dmod;
     std::vector<Request> reqs;
@@ -1724,6 +1865,59 @@ int pcsf_omega_score(pcsf_engine *e, pcsf_batch *b, double omega_h1, double sigm
     if (!(omega_h1 >= 0.0) || !(sigma_h1 >= 0.0))
         return e->fail(PCSF_EINVAL, "CamlPaml.P14n.instantiate_q: domain violation (omega_H1, sigma_H1 must be >= 0)");
     return omega_impl(e, b, omega_h1, sigma_h1, out);
+}
+
+int pcsf_omega_grad(pcsf_engine *e, pcsf_batch *b, const double *kappa, const double *omega, double sigma,
+                    const double *rho, double *lpr, double *d_branch, double *d_rho, double *d_kappa, double *d_omega,
+                    int32_t *status)
+{
+    if (!e) return PCSF_EINVAL;
+    CK(cudaSetDevice(e->device), "cudaSetDevice");
+    if (!b || b->e != e) return e->fail(PCSF_EINVAL, "pcsf_omega_grad: batch does not belong to this engine");
+    const int nreg = b->nreg;
+    if (nreg > 0 && (!kappa || !omega || !rho || !lpr)) return e->fail(PCSF_EINVAL, "pcsf_omega_grad: null argument");
+    if (!(sigma >= 0.0)) return e->fail(PCSF_EINVAL, "CamlPaml.P14n.instantiate_q: domain violation (sigma must be >= 0)");
+    if (nreg == 0) return PCSF_OK;
+    std::vector<std::array<double, 9>> f;
+    int rc = region_f3x4(e, b, f);
+    if (rc) return rc;
+    std::vector<OmegaKey> keys(nreg);
+    std::vector<Request> reqs(nreg);
+    for (int r = 0; r < nreg; r++) {
+        if (!(kappa[r] > 0.0) || !(omega[r] > 0.0) || !(rho[r] > 0.0) || !std::isfinite(rho[r]))
+            return e->fail(PCSF_EINVAL, "pcsf_omega_grad: region %d: kappa, omega and rho must be > 0", r);
+        keys[r][0] = kappa[r];
+        keys[r][1] = omega[r];
+        keys[r][2] = sigma;
+        for (int k = 0; k < 9; k++) keys[r][3 + k] = f[r][k];
+        reqs[r] = Request{r, r, 0, 0, rho[r]};     // request r uses the round's model r
+    }
+    DynModels dmod;
+    std::vector<int> slot;
+    rc = dyn_prepare(e, dmod, keys, slot);
+    if (rc) return rc;
+    DynGrad dg{};
+    rc = dyn_derivs(e, dmod, keys, slot, dg);
+    if (rc) return rc;
+    std::vector<Eval> res;
+    std::vector<double> g;
+    rc = evaluate(e, b, reqs, res, &g, false, &dmod.dm, nullptr, &dg);
+    if (rc) return rc;
+    const int gs = e->nbr + 2;
+    for (int r = 0; r < nreg; r++) {
+        lpr[r] = res[r].lpr;
+        if (status) status[r] = res[r].status;
+        double dr = 0.0;
+        for (int c = 0; c < e->nbr; c++) {
+            const double gc = g[(size_t)r * gs + c];
+            if (d_branch) d_branch[(size_t)r * e->nbr + c] = gc;
+            dr += e->branch[c] * gc;
+        }
+        if (d_rho) d_rho[r] = dr;
+        if (d_kappa) d_kappa[r] = g[(size_t)r * gs + e->nbr];
+        if (d_omega) d_omega[r] = g[(size_t)r * gs + e->nbr + 1];
+    }
+    return PCSF_OK;
 }
 
 void pcsf_engine_destroy(pcsf_engine *e)

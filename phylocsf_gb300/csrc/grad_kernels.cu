@@ -28,7 +28,7 @@ constexpr int GR_THREADS = 256;
 
 template <typename T, int TC>
 struct GradLayout {
-    static size_t smem(int nslots, int nl, int nint)
+    __host__ __device__ static size_t base(int nslots, int nl, int nint)
     {
         size_t b = sizeof(T) * (3 * (size_t)K2 + (size_t)nslots * K * TC + (size_t)K * TC + 16 * TC);
         b += sizeof(typename AtomMax<T>::U) * TC;
@@ -38,12 +38,23 @@ struct GradLayout {
         b += (size_t)nl * TC;
         return (b + 15) & ~size_t(15);
     }
-    static size_t scratch(int nl)
+    // parameter derivatives need U (appended) and two [K][TC] tiles, kept in the partial
+    // slots (idle during the outside pass) when there are at least two, else appended
+    // too; H_x^T uses Mat[1], which the outside pass does not touch
+    static size_t extra(int nslots, int npar)
+    {
+        if (!npar) return 0;
+        return sizeof(T) * ((size_t)K2 + (nslots >= 2 ? 0 : 2 * (size_t)K * TC));
+    }
+    static size_t smem(int nslots, int nl, int nint, int npar) { return base(nslots, nl, nint) + extra(nslots, npar); }
+    static size_t scratch(int nl, int npar)
     {
         const int n = 2 * nl - 1;
         size_t b = sizeof(T) * ((size_t)(n - 1) + (nl - 1)) * K * TC;
         b += sizeof(int) * 2 * (size_t)n * TC;
-        return (b + 255) & ~size_t(255);
+        b = (b + 255) & ~size_t(255);
+        if (npar) b += (sizeof(T) * (size_t)(nl - 1) * K * TC + 255) & ~size_t(255);   // alpha of internal nodes
+        return b;
     }
 };
 
@@ -64,6 +75,13 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad(GradArgs a)
     SchedNode *sched = reinterpret_cast<SchedNode *>(sexp + TC);   // [n_internal]
     size_t off = (reinterpret_cast<unsigned char *>(sched + a.n_internal) - gsm + 15) & ~size_t(15);
     uint8_t *lvT = gsm + off;                                      // [nl][TC]
+    // parameter derivatives (outside pass only): U and the eigenbasis images of inter and
+    // alpha_c over the slots (continuing past them into the extra space at the end of the
+    // layout when the slots are fewer), H_x^T in Mat[1]
+    T *Ubuf = reinterpret_cast<T *>(gsm + GradLayout<T, TC>::base(a.nslots, a.nl, a.n_internal));   // [K][K]
+    T *Pt = (a.nslots >= 2) ? slots : Ubuf + K2;                   // [K][TC]
+    T *Qt = Pt + K * TC;                                           // [K][TC]
+    T *Hbuf = Mat + K2;                                            // [K][K]
     __shared__ double wsum_l[GR_THREADS / 32], wsum_e[GR_THREADS / 32];
 
     const int tid = threadIdx.x;
@@ -75,6 +93,9 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad(GradArgs a)
     T *B = V + (size_t)(n - 1) * K * TC;                             // [nl-1][K][TC] (internal nodes)
     int *eS = reinterpret_cast<int *>(B + (size_t)(nl - 1) * K * TC);  // [n][TC]
     int *fS = eS + (size_t)n * TC;                                   // [n][TC]
+    T *Ascr = reinterpret_cast<T *>(sbase + ((sizeof(T) * ((size_t)(n - 1) + (nl - 1)) * K * TC +
+                                              sizeof(int) * 2 * (size_t)n * TC + 255) & ~size_t(255)));   // [nl-1][K][TC]
+    const int gstride = a.nbr + a.npar;
     auto e_of = [&](int node, int col) -> int { return node < nl ? 0 : eS[(size_t)node * TC + col]; };
 
     for (int f = tid; f < a.n_internal; f += GR_THREADS) sched[f] = a.sched[f];
@@ -95,7 +116,12 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad(GradArgs a)
         {
             const T *Qg = reinterpret_cast<const T *>(a.Qrow) + (size_t)md * K2;
             for (int f = tid; f < K2; f += GR_THREADS) Mat[2 * K2 + f] = Qg[f];
+            if (a.npar) {
+                const T *Ug = reinterpret_cast<const T *>(a.Umat) + (size_t)md * K2;
+                for (int f = tid; f < K2; f += GR_THREADS) Ubuf[f] = Ug[f];
+            }
         }
+        double pacc[2] = {0.0, 0.0};      // this work item's parameter derivatives (thread 0)
 
         // ---------------- inside pass, storing the child partials
         for (int ni = 0; ni < a.n_internal; ni++) {
@@ -142,7 +168,11 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad(GradArgs a)
                 T mx = AtomMax<T>::get(colmax + c0 + cc);
                 int e = (mx > (T)0) ? exp_of(mx) : 0;
 #pragma unroll
-                for (int i = 0; i < 4; i++) out[(a0 + i) * TC + c0 + cc] = scale2(vl[i][cc], -e);
+                for (int i = 0; i < 4; i++) {
+                    const T x = scale2(vl[i][cc], -e);
+                    out[(a0 + i) * TC + c0 + cc] = x;
+                    if (a.npar) Ascr[((size_t)(sn.node - nl) * K + a0 + i) * TC + c0 + cc] = x;
+                }
                 if (ty == 0) {
                     const int col = c0 + cc;
                     eS[(size_t)sn.node * TC + col] = e_of(sn.lc, col) + e_of(sn.rc, col) + e;
@@ -272,29 +302,90 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad(GradArgs a)
                 if (tid == 0) {
                     double g = 0.0;
                     for (int k = 0; k < (TC + 31) / 32; k++) g += wsum_l[k];
-                    a.gpart[(size_t)w * a.nbr + c] = g;
+                    a.gpart[(size_t)w * gstride + c] = g;
+                }
+                if (a.npar) {
+                    // inter^T (dP_c / dx) alpha_c = p^T H_x q with p = U^T D^-1/2 inter, q = U^T D^1/2 alpha_c
+                    const double *sqd = a.m.sq + md * K, *isqd = a.m.isq + md * K;
+                    __syncthreads();   // wsum_l, red read; X still holds inter
+                    for (int f = tid; f < K * TC; f += GR_THREADS) Qt[f] = X[f] * (T)isqd[f / TC];
+                    __syncthreads();
+                    T pv[4][CPT];
+                    contract<T, TC, KAHAN>(Ubuf, Qt, a0, c0, pv);
+                    __syncthreads();
+                    if (internal) {
+                        const T *Ac = Ascr + (size_t)(c - nl) * K * TC;
+                        for (int f = tid; f < K * TC; f += GR_THREADS) Qt[f] = Ac[f] * (T)sqd[f / TC];
+                    } else {
+                        for (int f = tid; f < K * TC; f += GR_THREADS) {
+                            const int st = f / TC, col = f % TC;
+                            const int sl = lvT[c * TC + col];
+                            Qt[f] = (sl >= K) ? (T)sqd[st] : (sl == st ? (T)sqd[st] : (T)0);
+                        }
+                    }
+                    __syncthreads();
+                    {
+                        T qv[4][CPT];
+                        contract<T, TC, KAHAN>(Ubuf, Qt, a0, c0, qv);
+#pragma unroll
+                        for (int i = 0; i < 4; i++)
+#pragma unroll
+                            for (int cc = 0; cc < CPT; cc++) Pt[(a0 + i) * TC + c0 + cc] = qv[i][cc];
+                    }
+                    for (int x = 0; x < a.npar; x++) {
+                        const T *Hg = reinterpret_cast<const T *>(a.Hmat) +
+                                      (((size_t)rq.pset * a.nbr + c) * a.npar + x) * K2;
+                        for (int f = tid; f < K2; f += GR_THREADS) Hbuf[f] = Hg[f];
+                        __syncthreads();   // Hbuf and the q tile (Pt) ready
+                        T rv[4][CPT];
+                        contract<T, TC, KAHAN>(Hbuf, Pt, a0, c0, rv);
+#pragma unroll
+                        for (int cc = 0; cc < CPT; cc++) {
+                            T acc = (T)0;
+#pragma unroll
+                            for (int i = 0; i < 4; i++) acc += pv[i][cc] * rv[i][cc];
+                            red[ty * TC + c0 + cc] = acc;
+                        }
+                        __syncthreads();
+                        double gx = 0.0;
+                        if (tid < TC && tid < ncols && zt[tid] > 0.0) {
+                            double sum = 0.0;
+                            for (int k = 0; k < 16; k++) sum += (double)red[k * TC + tid];
+                            const int ex = fS[(size_t)p * TC + tid] + e_of(s, tid) + e_of(c, tid) - eroot[tid];
+                            gx = ldexp(sum, ex) / zt[tid];
+                        }
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) gx += __shfl_down_sync(0xffffffffu, gx, o);
+                        if ((tid & 31) == 0) wsum_l[tid >> 5] = gx;
+                        __syncthreads();
+                        if (tid == 0)
+                            for (int k = 0; k < (TC + 31) / 32; k++) pacc[x] += wsum_l[k];
+                        __syncthreads();   // Hbuf, red, wsum_l free
+                    }
                 }
             }
         }
+        if (a.npar && tid == 0)
+            for (int x = 0; x < a.npar; x++) a.gpart[(size_t)w * gstride + a.nbr + x] = pacc[x];
     }
 }
 
-size_t grad_scratch_per_cta(int prec, int nl)
+size_t grad_scratch_per_cta(int prec, int nl, int npar)
 {
-    if (prec == PCSF_PREC_FP64) return GradLayout<double, 32>::scratch(nl);
-    return GradLayout<float, 64>::scratch(nl);
+    if (prec == PCSF_PREC_FP64) return GradLayout<double, 32>::scratch(nl, npar);
+    return GradLayout<float, 64>::scratch(nl, npar);
 }
 
-size_t grad_smem_bytes(int prec, int nslots, int nl, int nint)
+size_t grad_smem_bytes(int prec, int nslots, int nl, int nint, int npar)
 {
-    if (prec == PCSF_PREC_FP64) return GradLayout<double, 32>::smem(nslots, nl, nint);
-    return GradLayout<float, 64>::smem(nslots, nl, nint);
+    if (prec == PCSF_PREC_FP64) return GradLayout<double, 32>::smem(nslots, nl, nint, npar);
+    return GradLayout<float, 64>::smem(nslots, nl, nint, npar);
 }
 
 template <typename T, int TC, int KAHAN>
 static cudaError_t launch_grad_t(const GradArgs &a, cudaStream_t s, int grid)
 {
-    size_t smem = GradLayout<T, TC>::smem(a.nslots, a.nl, a.n_internal);
+    size_t smem = GradLayout<T, TC>::smem(a.nslots, a.nl, a.n_internal, a.npar);
     cudaError_t e = cudaFuncSetAttribute(k_grad<T, TC, KAHAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_grad<T, TC, KAHAN><<<grid, GR_THREADS, smem, s>>>(a);
@@ -308,6 +399,42 @@ cudaError_t launch_grad(int prec, int comp, const GradArgs &a, cudaStream_t s, i
     if (comp == 1) return launch_grad_t<float, 64, 1>(a, s, grid);
     if (comp == 2) return launch_grad_t<float, 64, 2>(a, s, grid);
     return launch_grad_t<float, 64, 0>(a, s, grid);
+}
+
+// H_x^T = (F(t) o Bdot_x)^T per (P set, branch, parameter).  F_ij = (e^{lam_i t} -
+// e^{lam_j t}) / (lam_i - lam_j), written as e^{lam_j t} (e^{d t} - 1) / d with
+// d = lam_i - lam_j and a Taylor series in d t when |d t| < 1e-2 (no cancellation).
+template <typename T>
+__global__ void __launch_bounds__(256) k_hform(const PSet *ps, const double *branch, int nbr, const double *lam,
+                                               const T *Bdot, T *H)
+{
+    __shared__ double el[K];
+    const int b = blockIdx.x, r = blockIdx.y, tid = threadIdx.x;
+    const PSet rq = ps[r];
+    const int md = rq.model;
+    const double t = rq.rho * branch[b];
+    const double *lm = lam + (size_t)md * K;
+    if (tid < K) el[tid] = exp(lm[tid] * t);
+    __syncthreads();
+    for (int f = tid; f < K2; f += 256) {
+        const int i = f / K, j = f % K;
+        const double d = lm[i] - lm[j], dt = d * t;
+        double F;
+        if (fabs(dt) < 1e-2) F = t * el[j] * (1.0 + dt * (0.5 + dt * (1.0 / 6.0 + dt * (1.0 / 24.0 + dt / 120.0))));
+        else F = (el[i] - el[j]) / d;
+        for (int x = 0; x < 2; x++)
+            H[(((size_t)r * nbr + b) * 2 + x) * K2 + (size_t)j * K + i] = (T)(F * (double)Bdot[((size_t)md * 2 + x) * K2 + f]);
+    }
+}
+
+cudaError_t launch_hform(bool fp64, const PSet *ps, int nps, const double *branch, int nbr, const double *lam,
+                         const void *Bdot, void *H, cudaStream_t s)
+{
+    if (nps <= 0) return cudaSuccess;
+    dim3 grid(nbr, nps);
+    if (fp64) k_hform<double><<<grid, 256, 0, s>>>(ps, branch, nbr, lam, (const double *)Bdot, (double *)H);
+    else k_hform<float><<<grid, 256, 0, s>>>(ps, branch, nbr, lam, (const float *)Bdot, (float *)H);
+    return cudaGetLastError();
 }
 
 // grad[r][c] = sum of gpart over request r's work items (fixed order)

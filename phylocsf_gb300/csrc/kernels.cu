@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
                 ex[tid] = expm1(lam[tid] * t);
                 cf[tid] = ex[tid];
             } else {
-                ex[tid] = (wrow[tid] != 0.0) ? expm1(lam[tid] * t) : 0.0;
+                ex[tid] = (wrow[tid] != 0.0) ? (double)expm1f((float)(lam[tid] * t)) : 0.0;   // row-sum check only
                 if (mode == 3) {
                     // e^{lam t_g} (tabulated) * expm1(lam (t - t_g)) in FP32: the
                     // coefficient is rounded to FP32 for the GEMM in any case
@@ -285,14 +285,15 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
             // biases lpr by ~1e-4 nats per 3000 codons at rho = 1
             bool neg = false;
             T diag = (T)0, dc = (T)0;
+            const T ntol = (T)(-m.tol), dtol = (T)(-1.0 - m.tol);
             for (int j = 0; j < K; j++) {
                 T x = Es[i * (K + 1) + j];
                 if (j == i) {
-                    if ((double)x + 1.0 < 0.0 && -((double)x + 1.0) > m.tol) neg = true;
+                    if (x < dtol) neg = true;      // x + 1 < -tol
                     continue;
                 }
                 if (x < (T)0) {
-                    if (-(double)x > m.tol) neg = true;
+                    if (x < ntol) neg = true;
                     x = (T)0;
                     Es[i * (K + 1) + j] = x;
                 }
@@ -307,7 +308,7 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
             }
             if (neg) status_min(status_key + r, b, i, PCSF_ENEGP);
             else if (fabs(rs) > m.tol) status_min(status_key + r, b, i, PCSF_EROWSUM);
-            else if (!((double)diag > -1.0)) status_min(status_key + r, b, i, PCSF_EDIAG);
+            else if (!(diag > (T)-1)) status_min(status_key + r, b, i, PCSF_EDIAG);
             Es[i * (K + 1) + i] = diag;
         }
         __syncthreads();
@@ -450,8 +451,13 @@ __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
     const int a0 = 4 * ty, c0 = CPT * tx;
     const int nl = a.nl;
     __shared__ double red_l[PR_THREADS / 32], red_e[PR_THREADS / 32];
+    __shared__ double ltab[256];           // log(1 + k/256), the dither factors' logs
+    __shared__ double dsum[TC];            // per column: sum over leaves of log c
+    const bool dith = a.dither && sizeof(T) == 4;
 
     for (int f = tid; f < a.n_internal; f += PR_THREADS) sched[f] = a.sched[f];
+    if (dith)
+        for (int f = tid; f < 256; f += PR_THREADS) ltab[f] = log1p((double)f / 256.0);
 
     for (int w = blockIdx.x; w < a.nwi; w += gridDim.x) {
         const WorkItem wi = a.wi[w];
@@ -467,6 +473,17 @@ __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
         }
         for (int f = tid; f < 2 * TC; f += PR_THREADS) colmax[f] = 0;
         for (int f = tid; f < TC; f += PR_THREADS) cscale[f] = 0;
+        // dither keys are the column's position within its region, so that results
+        // do not depend on where a region sits in the batch
+        const int64_t dcol0 = dith ? (int64_t)(uint32_t)((uint32_t)wi.col0 - rq.start) : -1;
+        if (dith) {
+            __syncthreads();   // ltab ready
+            for (int c = tid; c < TC; c += PR_THREADS) {
+                double sd = 0.0;
+                for (int l = 0; l < nl; l++) sd += ltab[dither_k(dcol0 + c, l)];
+                dsum[c] = sd;
+            }
+        }
 
         for (int ni = 0; ni < a.n_internal; ni++) {
             const SchedNode sn = sched[ni];
@@ -483,8 +500,8 @@ __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
             }
             __syncthreads();
             T vl[4][CPT], vr[4][CPT];
-            child_partial<T, TC, KAHAN>(Et, slots, sn.lslot, sn.lc, lvT, a0, c0, vl);
-            child_partial<T, TC, KAHAN>(Et + K2, slots, sn.rslot, sn.rc, lvT, a0, c0, vr);
+            child_partial<T, TC, KAHAN>(Et, slots, sn.lslot, sn.lc, lvT, a0, c0, vl, dcol0);
+            child_partial<T, TC, KAHAN>(Et + K2, slots, sn.rslot, sn.rc, lvT, a0, c0, vr, dcol0);
             __syncthreads();
             MU *cm = colmax + (ni & 1) * TC;
             MU *cm_next = colmax + ((ni + 1) & 1) * TC;
@@ -524,7 +541,7 @@ __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
                 wz += x * wl[s];
             }
             if (z > 0.0) {
-                tl = log(z) + (double)cscale[tid] * 0.69314718055994530942;
+                tl = log(z) + (double)cscale[tid] * 0.69314718055994530942 - (dith ? dsum[tid] : 0.0);
                 te = wz / z;
             } else {
                 tl = -INFINITY;

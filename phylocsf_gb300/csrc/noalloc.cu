@@ -102,7 +102,7 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
     for (int r = 0; r < n_regions; r++) {
         const int64_t c0 = col_offsets[r], c1 = col_offsets[r + 1];
         if (c1 < c0) return pcsf_internal_fail(e, PCSF_EINVAL, "pcsf_lpr_noalloc: col_offsets not non-decreasing");
-        h_req[r] = Request{r, model, 0, 0, rho};
+        h_req[r] = Request{r, model, 0, (uint32_t)c0, rho};
         h_wib[r] = nwi;
         for (int64_t c = c0; c < c1; c += TC) {
             if (nwi >= NOALLOC_MAX_WORK)
@@ -150,6 +150,7 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
         pa.nslots = nslots;
         pa.m = m;
         pa.partials = d_part;
+        pa.dither = prec != PCSF_PREC_FP64;     // as pcsf_lpr, so both give the same values
         const bool tcprec = prec == PCSF_PREC_TF32X3 || prec == PCSF_PREC_TF32;
         ce = launch_prune(prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32, (comp == 0 && tcprec) ? 1 : comp, pa,
                           s, std::min(pgrid, nwi));

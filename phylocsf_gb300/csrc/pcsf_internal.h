@@ -32,7 +32,7 @@ struct Request {
     int32_t region;
     int32_t model;
     int32_t pset;
-    int32_t pad;
+    uint32_t start;    // low 32 bits of the region's first global column (set by the launcher)
     double rho;
 };
 
@@ -107,6 +107,7 @@ struct PruneArgs {
     double *partials;        // [nwi][2]
     const void *Bop;         // tensor-core kernel: per chunk-local P set, [nbop][hi, lo][64 x 64] B operands
     int nbop;                //   of the branches above internal nodes (node nl + k)
+    int dither;              // SIMT FP32 kernel: per-column dithering of the leaf partials (prune_common.cuh)
 };
 // comp: 0 plain FP32 sums, 1 Kahan, 2 blocked Kahan (see prune_common.cuh)
 cudaError_t launch_prune(int prec, int comp, const PruneArgs &a, cudaStream_t s, int grid);
@@ -127,15 +128,24 @@ struct GradArgs {
     int nbr;
     int nslots;
     DevModels m;
-    const void *Qrow;        // [2][K][K] Q row-major in the arithmetic type
+    const void *Qrow;        // [model][K][K] Q row-major in the arithmetic type
     void *scratch;           // gridDim.x * scratch_per_cta bytes
     size_t scratch_per_cta;
     double *partials;        // [nwi][2]
-    double *gpart;           // [nwi][nbr]
+    double *gpart;           // [nwi][nbr + npar]
+    // rate-matrix parameter derivatives (OmegaModel kappa, omega): d lpr / d x =
+    // sum_c sum_col inter_c^T (dP_c / dx) alpha_c / z, with dP/dx = D^-1/2 U (F o Bdot_x) U^T D^1/2
+    int npar;                // 0 or 2
+    const void *Hmat;        // [pset][nbr][npar][K][K] (F(t_c) o Bdot_x)^T, arithmetic type
+    const void *Umat;        // [model][K][K] U row-major, arithmetic type
 };
 cudaError_t launch_grad(int prec, int comp, const GradArgs &a, cudaStream_t s, int grid);
-size_t grad_scratch_per_cta(int prec, int nl);
-size_t grad_smem_bytes(int prec, int nslots, int nl, int nint);
+size_t grad_scratch_per_cta(int prec, int nl, int npar);
+size_t grad_smem_bytes(int prec, int nslots, int nl, int nint, int npar);
+// H_x = (F(t) o Bdot_x)^T for every (P set, branch, parameter): F_ij = (e^{lam_i t} - e^{lam_j t}) /
+// (lam_i - lam_j), t e^{lam_i t} on the diagonal (Frechet derivative of exp in the eigenbasis)
+cudaError_t launch_hform(bool fp64, const PSet *ps, int nps, const double *branch, int nbr, const double *lam,
+                         const void *Bdot, void *H, cudaStream_t s);
 cudaError_t launch_reduce_grad(const double *gpart, const int32_t *wi_begin, int nreq, int nbr, double *grad,
                                cudaStream_t s);
 

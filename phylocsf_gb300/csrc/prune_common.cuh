@@ -95,6 +95,23 @@ __device__ __forceinline__ double rowsum_minus_one(const DevModels &m, int md, i
     return rs * m.isq[md * K + i];
 }
 
+// Per-column dithering of the leaf partials (SIMT FP32 pruning): each leaf partial
+// of column col is scaled by the exact factor c = 1 + k/256, k = dither_k(col, leaf),
+// and sum_leaves log c is subtracted from the column's log-likelihood.  The values
+// are mathematically unchanged; the FP32 rounding errors of columns that share
+// sub-patterns (the same states below a node) stop being identical, so they no
+// longer add up linearly over thousands of columns.
+__device__ __forceinline__ int dither_k(int64_t col, int leaf)
+{
+    uint32_t h = (uint32_t)col * 0x9E3779B1u + (uint32_t)((uint64_t)col >> 32) * 0x7FEB352Du + (uint32_t)leaf * 0x85EBCA77u;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    h *= 0x297A2D39u;
+    h ^= h >> 15;
+    return (int)(h & 255u);
+}
+
 // exp_of(x): the e of frexp (x = m 2^e, m in [0.5, 1)) read from the exponent
 // field for normal x; frexp itself for zero, subnormals and non-finite x.
 __device__ __forceinline__ int exp_of(float x)
@@ -211,17 +228,20 @@ __device__ inline void contract(const T *M, const T *X, int a0, int c0, T out[4]
 // leaf in state s (1 for a marginalised leaf: P rows sum to 1).
 template <typename T, int TC, int KAHAN>
 __device__ inline void child_partial(const T *Et, const T *slots, int slot, int leaf, const uint8_t *lvT, int a0,
-                                     int c0, T v[4][TC / 16])
+                                     int c0, T v[4][TC / 16], int64_t dither_col0 = -1)
 {
     constexpr int CPT = TC / 16;
     if (slot < 0) {
 #pragma unroll
         for (int cc = 0; cc < CPT; cc++) {
             int s = lvT[leaf * TC + c0 + cc];
+            // with dithering, c * P[a][s] in one rounding (c exact, see dither_k)
+            const T c = (dither_col0 >= 0) ? (T)(1.0f + (float)dither_k(dither_col0 + c0 + cc, leaf) * (1.0f / 256.0f))
+                                           : (T)1;
 #pragma unroll
             for (int i = 0; i < 4; i++) {
                 int a = a0 + i;
-                v[i][cc] = (s >= K) ? (T)1 : (Et[s * K + a] + (a == s ? (T)1 : (T)0));
+                v[i][cc] = (s >= K) ? c : fma(Et[s * K + a], c, (a == s ? c : (T)0));
             }
         }
         return;

@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
     __shared__ float cmax[2][4][TD_M];
     __shared__ double red[3][TD_THREADS / 32];
     __shared__ int16_t bseq[TD_MAX_LEAVES];
+    __shared__ float blen[2 * TD_MAX_LEAVES];     // branch lengths b_c (FP32)
     __shared__ int nbseq_s;
 
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -132,6 +133,7 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
         nbseq_s = k;
     }
     for (int f = tid; f < a.n_internal; f += TD_THREADS) sched[f] = a.sched[f];
+    for (int f = tid; f < a.nbr; f += TD_THREADS) blen[f] = (float)branch[f];
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -184,6 +186,24 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
         tmem_ld16(tbase + lane_off + cols + s0, x);
         td_store_a(sm, site, s0, x);
     };
+    // leaf child c: P_c[:, s] for this thread's states (1 for a marginalised leaf)
+    auto leaf_col = [&](const float *Pbase, int c, float *v) {
+        const int st = lvT[c * TD_M + site];
+        const float4 *row = reinterpret_cast<const float4 *>(Pbase + (size_t)c * K2 + (size_t)(st < K ? st : 0) * K + s0);
+#pragma unroll
+        for (int j4 = 0; j4 < TD_NS / 4; j4++) {
+            float4 x = make_float4(1.f, 1.f, 1.f, 1.f);
+            if (st < K) {
+                x = __ldg(row + j4);
+                const int a0 = s0 + 4 * j4;
+                x.x += (st == a0) ? 1.0f : 0.0f;
+                x.y += (st == a0 + 1) ? 1.0f : 0.0f;
+                x.z += (st == a0 + 2) ? 1.0f : 0.0f;
+                x.w += (st == a0 + 3) ? 1.0f : 0.0f;
+            }
+            v[4 * j4] = x.x; v[4 * j4 + 1] = x.y; v[4 * j4 + 2] = x.z; v[4 * j4 + 3] = x.w;
+        }
+    };
     // x = A (hi + lo) + D(cols)
     auto add_d = [&](uint32_t cols, float *x) {
         float d[TD_NS], al[TD_NS];
@@ -218,68 +238,81 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
 
         for (int ni = 0; ni < a.n_internal && ok; ni++) {
             const SchedNode sn = sched[ni];
-            float v1[TD_NS], u1[TD_NS], v2[TD_NS], u2[TD_NS];
-            int nproc = 0;
-            int free_cols = -1;      // TMEM columns free for a leaf's Q v (a consumed child's slot)
-            // internal children first, then leaves
-            for (int pass = 0; pass < 2 && ok; pass++) {
-                for (int side = 0; side < 2 && ok; side++) {
-                    const int s = side ? sn.rslot : sn.lslot;
-                    const int c = side ? sn.rc : sn.lc;
-                    if ((pass == 0) != (s >= 0)) continue;
-                    float *v = nproc ? v2 : v1, *u = nproc ? u2 : u1;
-                    const float bc = (float)(branch[c]);
-                    if (nproc && __syncthreads_or(bad)) { ok = false; break; }   // the A operand is free
-                    if (s >= 0) {
-                        const uint32_t ca = 128u * s, cd = 128u * s + 64u;
-                        // v = alpha + E alpha   (D over alpha's columns)
-                        stage_slot(ca);
-                        if (!run_mma(ca, sBE, true)) { bad = true; }
-                        add_d(ca, v);
-                        if (__syncthreads_or(bad)) { ok = false; break; }
-                        // u = alpha' + E alpha'   (D over alpha''s columns); then E is no longer needed
-                        stage_slot(cd);
-                        if (!run_mma(cd, sBE, false)) { bad = true; }
-                        if (tid == 0 && !bad) issue_next_b();
-                        add_d(cd, u);
-                        if (__syncthreads_or(bad)) { ok = false; break; }
-                        // u += b_c Q v   (D over alpha's columns)
-                        td_store_a(sm, site, s0, v);
-                        if (!run_mma(ca, sQ, false)) { bad = true; }
-                        acc_d(ca, bc, u, false);
-                        free_cols = (int)ca;
-                    } else {
-                        const int st = lvT[c * TD_M + site];
-                        const float4 *row = reinterpret_cast<const float4 *>(Pbase + (size_t)c * K2 +
-                                                                             (size_t)(st < K ? st : 0) * K + s0);
-#pragma unroll
-                        for (int j4 = 0; j4 < TD_NS / 4; j4++) {
-                            float4 x = make_float4(1.f, 1.f, 1.f, 1.f);
-                            if (st < K) {
-                                x = __ldg(row + j4);
-                                const int a0 = s0 + 4 * j4;
-                                x.x += (st == a0) ? 1.0f : 0.0f;
-                                x.y += (st == a0 + 1) ? 1.0f : 0.0f;
-                                x.z += (st == a0 + 2) ? 1.0f : 0.0f;
-                                x.w += (st == a0 + 3) ? 1.0f : 0.0f;
-                            }
-                            v[4 * j4] = x.x; v[4 * j4 + 1] = x.y; v[4 * j4 + 2] = x.z; v[4 * j4 + 3] = x.w;
-                        }
-                        const uint32_t cs = free_cols >= 0 ? (uint32_t)free_cols : 128u * sn.oslot;
-                        td_store_a(sm, site, s0, v);
-                        if (!run_mma(cs, sQ, false)) { bad = true; }
-                        acc_d(cs, bc, u, true);
-                    }
-                    nproc++;
-                }
+            // v1 / u1: value and tangent of the first child, then of the node; vt: second child's value.
+            // Internal children first; the node's tangent is folded in as the second child's parts
+            // arrive (u_p = u_1 v_2 + v_1 u_2), which keeps three 16-value arrays live.
+            float v1[TD_NS], u1[TD_NS], vt[TD_NS];
+            const bool int0 = sn.lslot >= 0 || sn.rslot >= 0;        // is the first child internal?
+            const int cA = (sn.lslot >= 0 || sn.rslot < 0) ? sn.lc : sn.rc;
+            const int cB = (cA == sn.lc) ? sn.rc : sn.lc;
+            const int sA_ = (cA == sn.lc) ? sn.lslot : sn.rslot, sB_ = (cA == sn.lc) ? sn.rslot : sn.lslot;
+            const uint32_t scratch = int0 ? 128u * (uint32_t)sA_ : 128u * (uint32_t)sn.oslot;
+            // ---- first child
+            if (int0) {
+                const uint32_t ca = 128u * sA_, cd = ca + 64u;
+                stage_slot(ca);
+                if (!run_mma(ca, sBE, true)) bad = true;
+                add_d(ca, v1);                                   // v = alpha + E alpha
+                if (__syncthreads_or(bad)) { ok = false; break; }
+                stage_slot(cd);
+                if (!run_mma(cd, sBE, false)) bad = true;
+                if (tid == 0 && !bad) issue_next_b();
+                add_d(cd, u1);                                   // alpha' + E alpha'
+                if (__syncthreads_or(bad)) { ok = false; break; }
+                td_store_a(sm, site, s0, v1);
+                if (!run_mma(ca, sQ, false)) bad = true;
+                acc_d(ca, blen[cA], u1, false);                  // + b Q v
+            } else {
+                leaf_col(Pbase, cA, v1);
+                td_store_a(sm, site, s0, v1);
+                if (!run_mma(scratch, sQ, false)) bad = true;
+                acc_d(scratch, blen[cA], u1, true);              // u = b Q v
             }
-            if (!ok) break;
-            // alpha_p = v1 v2, alpha'_p = u1 v2 + v1 u2, rescaled together
+            if (__syncthreads_or(bad)) { ok = false; break; }    // the A operand is free again
+            // ---- second child
+            if (sB_ >= 0) {
+                const uint32_t ca = 128u * sB_, cd = ca + 64u;
+                stage_slot(ca);
+                if (!run_mma(ca, sBE, true)) bad = true;
+                add_d(ca, vt);
+#pragma unroll
+                for (int k = 0; k < TD_NS; k++) u1[k] *= vt[k];   // u_1 v_2
+                if (__syncthreads_or(bad)) { ok = false; break; }
+                stage_slot(cd);
+                if (!run_mma(cd, sBE, false)) bad = true;
+                if (tid == 0 && !bad) issue_next_b();
+                {
+                    float w[TD_NS];
+                    add_d(cd, w);
+#pragma unroll
+                    for (int k = 0; k < TD_NS; k++) u1[k] += v1[k] * w[k];   // v_1 (alpha' + E alpha')
+                }
+                if (__syncthreads_or(bad)) { ok = false; break; }
+                td_store_a(sm, site, s0, vt);
+                if (!run_mma(ca, sQ, false)) bad = true;
+                {
+                    float d[TD_NS];
+                    tmem_ld16(tbase + lane_off + ca + s0, d);
+                    const float bb = blen[cB];
+#pragma unroll
+                    for (int k = 0; k < TD_NS; k++) u1[k] += v1[k] * (bb * d[k]);   // v_1 b Q v_2
+                }
+            } else {
+                leaf_col(Pbase, cB, vt);
+#pragma unroll
+                for (int k = 0; k < TD_NS; k++) u1[k] *= vt[k];
+                td_store_a(sm, site, s0, vt);
+                if (!run_mma(scratch, sQ, false)) bad = true;
+                float d[TD_NS];
+                tmem_ld16(tbase + lane_off + scratch + s0, d);
+                const float bb = blen[cB];
+#pragma unroll
+                for (int k = 0; k < TD_NS; k++) u1[k] += v1[k] * (bb * d[k]);
+            }
             float mx = 0.0f;
 #pragma unroll
             for (int k = 0; k < TD_NS; k++) {
-                u1[k] = u1[k] * v2[k] + v1[k] * u2[k];
-                v1[k] = v1[k] * v2[k];
+                v1[k] *= vt[k];
                 mx = fmaxf(mx, v1[k]);
             }
             float (*cm)[TD_M] = cmax[ni & 1];

@@ -46,7 +46,8 @@ __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const 
     __shared__ float cfs[2][K];
     __shared__ double exs[2][K];        // expm1(lam_m t) where w_m != 0 (row-sum check)
     __shared__ int mode_g[PFT_MAX_BRANCHES];      // per branch: grid point << 2 | mode
-    __shared__ double t_b[PFT_MAX_BRANCHES];
+    __shared__ float t_b[PFT_MAX_BRANCHES];       // t (FP32: the Taylor branch and expm1f only)
+    __shared__ float h_b[PFT_MAX_BRANCHES];       // t - t_g, formed in FP64
 
     const int tid = threadIdx.x;
     const int r = blockIdx.x;           // P set (chunk-local)
@@ -98,22 +99,31 @@ __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const 
             if (g + 1 < m.grid_n && (m.grid_t[g + 1] - t) < (t - m.grid_t[g])) g++;
         }
         mode_g[b] = (g << 2) | mode;
-        t_b[b] = t;
+        t_b[b] = (float)t;
+        h_b[b] = (mode == 2) ? (float)(t - m.grid_t[g]) : 0.0f;
     }
+    // FP32 copies of this thread's eigenvalue and its stationary-direction flag
+    // (FP64 runs at a small fraction of the FP32 rate on this part)
+    const float lam_i = (float)lam[i];
+    bool listed = false;
+    {
+        const int16_t *wl = m.wlist + md * WLIST;
+        if (wl[0] == -2) listed = (wrow[i] != 0.0);
+        else
+            for (int k = 0; k < WLIST; k++) listed |= (wl[k] == i);
+    }
+    const float ntol = -(float)m.tol, dtol = (float)(-1.0 - m.tol);
 
     for (int b0 = 0; b0 < nbr; b0 += 2) {
         const int b = b0 + bsel;                      // this thread's branch
         if (__syncthreads_or(!ok)) break;             // per-branch table ready / previous pair done
         const int mode = (b < nbr) ? (mode_g[b] & 3) : 0, g = (b < nbr) ? (mode_g[b] >> 2) : 0;
-        const double t = (b < nbr) ? t_b[b] : 0.0;
+        const float t = (b < nbr) ? t_b[b] : 0.0f;
         {
             float cf = 0.0f;
-            if (mode == 2) {
-                const double h = t - m.grid_t[g];
-                cf = m.grid_eg[((size_t)md * m.grid_n + g) * K + i] * expm1f((float)(lam[i] * h));
-            }
+            if (mode == 2) cf = m.grid_eg[((size_t)md * m.grid_n + g) * K + i] * expm1f(lam_i * h_b[b]);
             cfs[bsel][i] = cf;      // thread (bsel, i) supplies coefficient m = i
-            exs[bsel][i] = (wrow[i] != 0.0) ? expm1(lam[i] * t) : 0.0;
+            exs[bsel][i] = listed ? (double)expm1f(lam_i * t) : 0.0;
         }
         __syncthreads();
         // ---- A operand: row tid = isq_i U_im cf_m, TF32 hi / lo
@@ -152,7 +162,7 @@ __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const 
         {
             const float *eg = m.gridT + ((size_t)md * m.grid_n + g) * K2;   // E(t_g)^T
             const float *Qf = m.Qf + (size_t)md * K2 + (size_t)i * K, *Q2f = m.Q2f + (size_t)md * K2 + (size_t)i * K;
-            const float tt = (float)t, h2 = (float)(0.5 * t * t);
+            const float tt = t, h2 = 0.5f * t * t;
 #pragma unroll
             for (int j = 0; j < K; j++) {
                 if (mode == 2) row[j] = __ldg(eg + (size_t)j * K + i);
@@ -182,11 +192,11 @@ __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const 
             for (int j = 0; j < K; j++) {
                 float x = row[j];
                 if (j == i) {
-                    if ((double)x + 1.0 < 0.0 && -((double)x + 1.0) > m.tol) neg = true;
+                    if (x < dtol) neg = true;
                     continue;
                 }
                 if (x < 0.0f) {
-                    if (-(double)x > m.tol) neg = true;
+                    if (x < ntol) neg = true;
                     x = 0.0f;
                     row[j] = 0.0f;
                 }
@@ -201,7 +211,7 @@ __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const 
             const double rs = rowsum_minus_one(m, md, i, exs[bsel]);
             if (neg) status_min(status_key + r, b, i, PCSF_ENEGP);
             else if (fabs(rs) > m.tol) status_min(status_key + r, b, i, PCSF_EROWSUM);
-            else if (!((double)diag > -1.0)) status_min(status_key + r, b, i, PCSF_EDIAG);
+            else if (!(diag > -1.0f)) status_min(status_key + r, b, i, PCSF_EDIAG);
             if (b >= nl) {      // above an internal node: the pruning kernel's B operand
                 float *dst = Bop + ((size_t)r * (nbr - nl) + (b - nl)) * 2 * K2;
 #pragma unroll

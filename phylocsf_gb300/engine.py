@@ -95,6 +95,7 @@ SIGNATURES = {
                              ctypes.c_int),
     "pcsf_engine_create_tree": ([ctypes.POINTER(_Tree), ctypes.c_int32, ctypes.POINTER(_VP)], ctypes.c_int),
     "pcsf_omega_score": ([_VP, _VP, ctypes.c_double, ctypes.c_double, ctypes.POINTER(OmegaResult)], ctypes.c_int),
+    "pcsf_omega_grad": ([_VP, _VP, _D, _D, ctypes.c_double, _D, _D, _D, _D, _D, _D, _I32], ctypes.c_int),
     "pcsf_engine_destroy": ([_VP], None),
     "pcsf_last_error": ([_VP], ctypes.c_char_p),
     "pcsf_engine_get_stats": ([_VP, ctypes.POINTER(Stats)], ctypes.c_int),
@@ -276,6 +277,21 @@ class Batch:
                                      _p(lv, ctypes.c_uint8), ctypes.byref(h)), engine.handle)
         self.handle = h
 
+    def omega_grad(self, batch: Batch, kappa, omega, rho, sigma: float = 1.0, branches: bool = True) -> dict:
+        """OmegaModel log-likelihood and its gradient at per-region (kappa, omega, rho): keys lpr,
+        d_branch (or None), d_rho, d_kappa, d_omega, status (pcsf_omega_grad)."""
+        n = batch.n_regions
+        arr = lambda v: np.ascontiguousarray(np.broadcast_to(np.asarray(v, np.float64), (n,)))
+        k, o, r = arr(kappa), arr(omega), arr(rho)
+        out = {"lpr": np.zeros(n), "d_rho": np.zeros(n), "d_kappa": np.zeros(n), "d_omega": np.zeros(n),
+               "status": np.zeros(n, np.int32),
+               "d_branch": np.zeros((n, self.tree.n - 1)) if branches else None}
+        D = lambda a: _p(a, ctypes.c_double) if a is not None else None
+        _check(self.lib.pcsf_omega_grad(self.handle, batch.handle, D(k), D(o), sigma, D(r), D(out["lpr"]),
+                                        D(out["d_branch"]), D(out["d_rho"]), D(out["d_kappa"]), D(out["d_omega"]),
+                                        _p(out["status"], ctypes.c_int32)), self.handle)
+        return out
+
     def close(self):
         if getattr(self, "handle", None):
             self.engine.lib.pcsf_batch_destroy(self.handle)
@@ -328,6 +344,21 @@ class Engine:
         out = np.zeros(batch.n_regions, OMEGA_DTYPE)
         _check(self.lib.pcsf_omega_score(self.handle, batch.handle, omega_h1, sigma_h1,
                                          out.ctypes.data_as(ctypes.POINTER(OmegaResult))), self.handle)
+        return out
+
+    def omega_grad(self, batch: Batch, kappa, omega, rho, sigma: float = 1.0, branches: bool = True) -> dict:
+        """OmegaModel log-likelihood and its gradient at per-region (kappa, omega, rho): keys lpr,
+        d_branch (or None), d_rho, d_kappa, d_omega, status (pcsf_omega_grad)."""
+        n = batch.n_regions
+        arr = lambda v: np.ascontiguousarray(np.broadcast_to(np.asarray(v, np.float64), (n,)))
+        k, o, r = arr(kappa), arr(omega), arr(rho)
+        out = {"lpr": np.zeros(n), "d_rho": np.zeros(n), "d_kappa": np.zeros(n), "d_omega": np.zeros(n),
+               "status": np.zeros(n, np.int32),
+               "d_branch": np.zeros((n, self.tree.n - 1)) if branches else None}
+        D = lambda a: _p(a, ctypes.c_double) if a is not None else None
+        _check(self.lib.pcsf_omega_grad(self.handle, batch.handle, D(k), D(o), sigma, D(r), D(out["lpr"]),
+                                        D(out["d_branch"]), D(out["d_rho"]), D(out["d_kappa"]), D(out["d_omega"]),
+                                        _p(out["status"], ctypes.c_int32)), self.handle)
         return out
 
     def close(self):

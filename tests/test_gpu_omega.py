@@ -66,3 +66,49 @@ def test_omega_reference_example():
     g = e.omega_score(e.batch(np.array([0, lv.shape[0]], np.int64), H.oracle_leaves_to_u8(lv)))[0]
     sc = W.score(tree, lv)[0]
     assert g["status"] == 0 and abs(g["score"] - sc) <= 1e-6
+
+
+@pytest.mark.parametrize("name", ["12flies", "29mammals"])
+def test_omega_grad_matches_finite_differences(name):
+    """d lpr / d {kappa, omega, rho} from pcsf_omega_grad (adjoint + eigenbasis derivative of exp(tQ))
+    against central differences with h = 1e-5 of the FP64 engine's own lpr and of the oracle's:
+    within 1e-5 relative + 2e-4 absolute (the differences carry ~1e-12 relative evaluation noise over
+    2h); lpr itself within 1e-9 relative of the oracle."""
+    ps, offs, leaves = _regions(name, [40, 120], seed=29)
+    tree, *_ = H.fixture_params(name)
+    e = P.Engine.for_tree(ps.tree, precision="fp64")
+    b = e.batch(offs, leaves)
+    kappa, omega, rho, sigma, h = 2.5, 0.3, 0.8, 1.0, 1e-5
+    g = e.omega_grad(b, kappa, omega, rho, sigma)
+    assert (g["status"] == 0).all()
+
+    def lpr_at(k, o, r):
+        return e.omega_grad(b, k, o, r, sigma, branches=False)["lpr"]
+
+    fd = {"d_kappa": (lpr_at(kappa + h, omega, rho) - lpr_at(kappa - h, omega, rho)) / (2 * h),
+          "d_omega": (lpr_at(kappa, omega + h, rho) - lpr_at(kappa, omega - h, rho)) / (2 * h),
+          "d_rho": (lpr_at(kappa, omega, rho + h) - lpr_at(kappa, omega, rho - h)) / (2 * h)}
+    for k, v in fd.items():
+        assert np.all(np.abs(g[k] - v) <= 1e-5 * np.abs(v) + 2e-4), (k, g[k], v)
+    assert np.allclose(g["d_branch"] @ tree.branch[: tree.n - 1], g["d_rho"], rtol=1e-12, atol=1e-12)
+    for r in range(len(offs) - 1):
+        lv = H.u8_to_oracle(leaves[offs[r]:offs[r + 1]])
+        obj = W._Objective(O.OTree(tree), np.ascontiguousarray(lv, np.int32))
+        q = [kappa, omega, sigma] + list(W.f3x4_from_leaves(lv))
+        assert g["lpr"][r] == pytest.approx(obj.lpr(q, rho), rel=1e-9)
+        for k, idx in (("d_kappa", 0), ("d_omega", 1)):
+            qp, qm = list(q), list(q)
+            qp[idx] += h
+            qm[idx] -= h
+            ofd = (obj.lpr(qp, rho) - obj.lpr(qm, rho)) / (2 * h)
+            assert abs(g[k][r] - ofd) <= 1e-5 * abs(ofd) + 2e-4, (k, r, g[k][r], ofd)
+
+
+def test_omega_grad_fp32_close_to_fp64():
+    ps, offs, leaves = _regions("29mammals", [150, 60], seed=31)
+    g64 = P.Engine.for_tree(ps.tree, precision="fp64")
+    g32 = P.Engine.for_tree(ps.tree, precision="fp32c")
+    a = g64.omega_grad(g64.batch(offs, leaves), 2.0, 0.5, 1.2, 0.01)
+    c = g32.omega_grad(g32.batch(offs, leaves), 2.0, 0.5, 1.2, 0.01)
+    for k in ("d_kappa", "d_omega", "d_rho"):
+        assert np.all(np.abs(c[k] - a[k]) <= 1e-3 * np.abs(a[k]) + 1e-2), (k, c[k], a[k])
