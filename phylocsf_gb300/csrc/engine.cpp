@@ -479,7 +479,7 @@ static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2],
                     const float x = (float)(e->U[m][j * K + mm] * e->sq[m][j]);
                     uint32_t bits;
                     std::memcpy(&bits, &x, 4);
-                    bits &= 0xFFFFE000u;
+                    bits = (bits + 0x1000u) & 0xFFFFE000u;   // nearest TF32 value
                     float hi;
                     std::memcpy(&hi, &bits, 4);
                     const size_t o = (size_t)m * 2 * K2 + (mm / 4) * 256 + j * 4 + mm % 4;
@@ -494,7 +494,7 @@ static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2],
                     const float x = (float)Q[m][aa * K + j];
                     uint32_t bits;
                     std::memcpy(&bits, &x, 4);
-                    bits &= 0xFFFFE000u;
+                    bits = (bits + 0x1000u) & 0xFFFFE000u;   // nearest TF32 value
                     float hi;
                     std::memcpy(&hi, &bits, 4);
                     const size_t o = (size_t)m * 2 * K2 + (j / 4) * 256 + aa * 4 + j % 4;
@@ -883,6 +883,10 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
 // adjoint pass (second-order remainder < 1e-8 relative); every reported value
 // is still a direct evaluation.
 constexpr double DERIV_REL = 1e-4;
+// Noise band of a tensor-core search comparison: inside it the compensated kernel decides.
+// (measured: the tensor-core error of a difference of nearby points has a standard
+// deviation of ~3.3e-6 nats x sqrt(columns); the band is three of those)
+constexpr double AMBIGUOUS_PER_SQRT_COL = 1e-5;
 
 struct Fit {
     int region = 0, model = 0;
@@ -1055,6 +1059,7 @@ static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need
         }
         case Fit::BR_ACCEPT: {
             double fu;
+            bool better;
             const double u = f.u;
             if (f.deriv && std::fabs(u - f.bx) <= DERIV_REL * std::fabs(f.bx) && f.ncols > 0) {
                 const Eval *bx = f.get(f.bx);
@@ -1065,13 +1070,31 @@ static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need
                 }
                 if (failed(bx)) return;
                 fu = -(bx->lpr + (*g) * (u - f.bx));
+                better = fu <= f.bfx;
             } else {
                 const Eval *a = ask(u);
                 if (!a) return;
                 if (failed(a)) return;
                 fu = -a->lpr;
+                better = fu <= f.bfx;
+                // search values from the tensor cores: a comparison inside their noise band is
+                // decided by the compensated kernel's values of both points instead (the state
+                // keeps the search values, so later comparisons stay like for like)
+                if (f.accurate_final && f.ncols > 0 &&
+                    std::fabs(fu - f.bfx) <= AMBIGUOUS_PER_SQRT_COL * std::sqrt((double)f.ncols)) {
+                    const Eval *au = nullptr, *ax = nullptr;
+                    for (auto &c : f.acache) {
+                        if (c.first == u) au = &c.second;
+                        if (c.first == f.bx) ax = &c.second;
+                    }
+                    if (!au) need_acc.push_back(u);
+                    if (!ax) need_acc.push_back(f.bx);
+                    if (!au || !ax) return;
+                    if (failed(au) || failed(ax)) return;
+                    better = -au->lpr <= -ax->lpr;
+                }
             }
-            if (fu <= f.bfx) {
+            if (better) {
                 if (u < f.bx) { f.bhi = f.bx; f.bfhi = f.bfx; }
                 else { f.blo = f.bx; f.bflo = f.bfx; }
                 f.v = f.w; f.fv = f.fw;

@@ -68,10 +68,11 @@ __device__ __forceinline__ void status_min(int32_t *key, int branch, int row, in
 // element (a, j) at float offset (j/4)*256 + a*4 + j%4 of its part.
 __device__ __forceinline__ void bop_store(float *dst, int a, int q, float4 x)
 {
-    const float4 h = make_float4(__uint_as_float(__float_as_uint(x.x) & 0xFFFFE000u),
-                                 __uint_as_float(__float_as_uint(x.y) & 0xFFFFE000u),
-                                 __uint_as_float(__float_as_uint(x.z) & 0xFFFFE000u),
-                                 __uint_as_float(__float_as_uint(x.w) & 0xFFFFE000u));
+    // hi rounded to the nearest TF32 value (as tf32_hi in tc_common.cuh), lo = x - hi exact
+    const float4 h = make_float4(__uint_as_float((__float_as_uint(x.x) + 0x1000u) & 0xFFFFE000u),
+                                 __uint_as_float((__float_as_uint(x.y) + 0x1000u) & 0xFFFFE000u),
+                                 __uint_as_float((__float_as_uint(x.z) + 0x1000u) & 0xFFFFE000u),
+                                 __uint_as_float((__float_as_uint(x.w) + 0x1000u) & 0xFFFFE000u));
     const float4 l = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
     *reinterpret_cast<float4 *>(dst + q * 256 + a * 4) = h;
     *reinterpret_cast<float4 *>(dst + K2 + q * 256 + a * 4) = l;

@@ -73,7 +73,10 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
     return done != 0;
 }
 
-__device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+// hi part of the TF32 split x = hi + lo: x rounded to the nearest TF32 value (ties away
+// from zero), so lo = x - hi (exact in FP32) takes either sign and the bits of lo the
+// MMA drops (it reads 10 mantissa bits) cancel on average instead of always shrinking |x|
+__device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u); }
 
 // one bulk copy global -> shared of `bytes` (a multiple of 16, both addresses
 // 16-byte aligned), completing on mbarrier bar, which expects those bytes

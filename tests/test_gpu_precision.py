@@ -1,0 +1,59 @@
+"""Precision of the split-precision contractions on the 120mammals workload (238 branches,
+2 M codon columns in alignments of 100-5000 codons, rho = 1), against the FP64 GPU path
+(itself within 1e-9 relative of the FP64 oracle, test_gpu_parity.py).
+
+Per alignment: relative logL error of each model and |d score| of the fixed-strategy
+score.  Bounds (the measured values are printed):
+  - tensor cores, TF32 single product (tf32_direct): relative logL error <= 2e-3;
+  - tensor cores, TF32 hi/lo x3 (tf32x3_direct): relative logL error <= 2e-6;
+  - returned values of the tensor-core engine (tf32x3b, compensated SIMT kernel) and the
+    compensated FP32 engines: |d score| <= 1e-3 dB for every alignment.
+A 3xBF16 split is not built (TF32x3 recovers the same ~22 bits with three products).
+"""
+import numpy as np
+import pytest
+
+import phylocsf_gb300 as P
+from phylocsf_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def workload():
+    return synth.workload_120mammals_fixed(total_cols=2_000_000, seed=0)
+
+
+@pytest.fixture(scope="module")
+def reference(workload):
+    ps = workload.params
+    e = P.Engine(ps.tree, ps.S_c, ps.pi_c, ps.S_n, ps.pi_n, precision="fp64")
+    b = e.batch(workload.col_offsets, workload.leaves)
+    out = (e.lpr(b, 0, 1.0)[0], e.lpr(b, 1, 1.0)[0])
+    e.close()
+    return out
+
+
+def _lprs(workload, prec):
+    ps = workload.params
+    e = P.Engine(ps.tree, ps.S_c, ps.pi_c, ps.S_n, ps.pi_n, precision=prec)
+    b = e.batch(workload.col_offsets, workload.leaves)
+    out = (e.lpr(b, 0, 1.0)[0], e.lpr(b, 1, 1.0)[0])
+    e.close()
+    return out
+
+
+@pytest.mark.parametrize("prec,rel_bound,db_bound", [("tf32_direct", 2e-3, None), ("tf32x3_direct", 2e-6, None),
+                                                     ("tf32x3b", None, 1e-3), ("fp32b", None, 1e-3),
+                                                     ("fp32c", None, 1e-3)])
+def test_120mammals_precision(workload, reference, prec, rel_bound, db_bound):
+    c64, n64 = reference
+    c, n = _lprs(workload, prec)
+    rel = np.maximum(np.abs(c - c64) / np.abs(c64), np.abs(n - n64) / np.abs(n64))
+    ddb = np.abs(10.0 * ((c - n) - (c64 - n64)) / np.log(10.0))
+    print("%s: %d alignments, relative logL error max %.3e median %.3e; |d score| max %.3e dB median %.3e dB"
+          % (prec, len(c), rel.max(), np.median(rel), ddb.max(), np.median(ddb)))
+    if rel_bound is not None:
+        assert rel.max() <= rel_bound
+    if db_bound is not None:
+        assert ddb.max() <= db_bound
