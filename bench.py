@@ -362,6 +362,32 @@ def run_ours(args, world, rank, local):
             "pruning_kernels": kinds,
             "clocks": clk}
 
+    if args.latency_batches > 0:
+        # serving view: the regions arrive as B consecutive batches (host buffers, one
+        # pcsf_score_batch call each); a region's latency is the time from the first
+        # submission until its batch's results are on the host
+        B = args.latency_batches
+        cuts = np.linspace(0, wl.n_regions, B + 1).astype(np.int64)
+        batch_ms, done_ms = [], []
+        torch.cuda.synchronize(local)
+        t_start = time.perf_counter()
+        for k in range(B):
+            r0, r1 = cuts[k], cuts[k + 1]
+            o = wl.col_offsets[r0:r1 + 1] - wl.col_offsets[r0]
+            lv = wl.leaves[wl.col_offsets[r0]:wl.col_offsets[r1]]
+            t0 = time.perf_counter()
+            eng.score_batch(np.ascontiguousarray(o), np.ascontiguousarray(lv), wl.strategy)
+            t1 = time.perf_counter()
+            batch_ms.append(1000 * (t1 - t0))
+            done_ms.extend([1000 * (t1 - t_start)] * int(r1 - r0))
+        total_s = time.perf_counter() - t_start
+        line["latency"] = {"batches": B, "regions_per_batch": int(wl.n_regions // B),
+                           "batch_ms_p50": float(np.percentile(batch_ms, 50)),
+                           "batch_ms_p99": float(np.percentile(batch_ms, 99)),
+                           "region_latency_ms_p50": float(np.percentile(done_ms, 50)),
+                           "region_latency_ms_p99": float(np.percentile(done_ms, 99)),
+                           "throughput_regions_per_s": wl.n_regions / total_s,
+                           "clock": "host wall clock around each call (synchronous API)"}
     if rank == 0 and not args.no_accuracy:
         acc = {}
         # (a) against the FP64 GPU path on a subsample
@@ -410,6 +436,8 @@ def main():
     ap.add_argument("--cpu-cores", type=int, default=0)
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--latency-batches", type=int, default=0,
+                    help="also score the workload as this many consecutive batches and report latency percentiles")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")

@@ -62,13 +62,17 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float *v)
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+// Each poll may suspend the thread for up to TC_WAIT_HINT_NS (it resumes as soon as
+// the phase completes), so waiting warps do not take issue slots from the co-resident
+// CTA; TC_WAIT_LIMIT polls bound the wait (~4 s).
+constexpr uint32_t TC_WAIT_HINT_NS = 1000;
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
 {
     uint32_t done = 0;
     for (long it = 0; it < TC_WAIT_LIMIT && !done; it++) {
-        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
                      " selp.u32 %0, 1, 0, p;\n}\n"
-                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+                     : "=r"(done) : "r"(bar), "r"(parity), "r"(TC_WAIT_HINT_NS) : "memory");
     }
     return done != 0;
 }
