@@ -112,3 +112,24 @@ def test_omega_grad_fp32_close_to_fp64():
     c = g32.omega_grad(g32.batch(offs, leaves), 2.0, 0.5, 1.2, 0.01)
     for k in ("d_kappa", "d_omega", "d_rho"):
         assert np.all(np.abs(c[k] - a[k]) <= 1e-3 * np.abs(a[k]) + 1e-2), (k, c[k], a[k])
+
+
+def test_gradient_map_beside_brent():
+    """The gradient MAP (omega_fit.gradient_map: batched projected BFGS on pcsf_omega_grad) reaches
+    at least the objective of the reference's Brent coordinate ascent (the H0 fit of
+    pcsf_omega_score, which stops at a 1 % bracket) on every region, and lands next to it."""
+    from phylocsf_gb300 import omega_fit
+    ps, offs, leaves = _regions("29mammals", [200, 350, 600, 80, 450, 260], seed=37)
+    e = P.Engine.for_tree(ps.tree, precision="fp64")
+    b = e.batch(offs, leaves)
+    brent = e.omega_score(b)
+    gm = omega_fit.gradient_map(e, b, omega=1.0, sigma=1.0)
+    assert (gm["status"] == 0).all()
+    # kr_map reports lpr + log p(kappa) from its last (kappa) step; add log p(rho) for the joint objective
+    brent_f = brent["lpr_h0"] + omega_fit.log_prior_rho(brent["rho_h0"])
+    gap = gm["objective"] - brent_f
+    print("gradient MAP - Brent objective:", gap, "evaluations:", gm["evals"], "Brent evals:", brent["evals"])
+    assert np.all(gap >= -1e-6 * np.abs(brent_f) - 1e-6), gap
+    assert np.all(gap <= 0.5), gap
+    assert np.allclose(gm["rho"], brent["rho_h0"], rtol=0.05)
+    assert np.allclose(gm["kappa"], brent["kappa_h0"], rtol=0.05)
