@@ -186,28 +186,25 @@ __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const 
         }
         tc_fence_before();
         if (b < nbr && done) {
+            // branch-free in j: i differs per lane, and a branch on j == i would split the
+            // warp into single-lane paths for everything that follows
             bool neg = false;
             float diag = 0.0f, dc = 0.0f;
 #pragma unroll
             for (int j = 0; j < K; j++) {
-                float x = row[j];
-                if (j == i) {
-                    if (x < dtol) neg = true;
-                    continue;
-                }
-                if (x < 0.0f) {
-                    if (x < ntol) neg = true;
-                    x = 0.0f;
-                    row[j] = 0.0f;
-                }
-                const float y = -x - dc;       // Kahan: diag -= x
+                const bool dj = (j == i);
+                const float x0 = row[j];
+                neg |= dj ? (x0 < dtol) : (x0 < ntol);
+                const float x = fmaxf(x0, 0.0f);          // clamp an off-diagonal negative
+                row[j] = dj ? x0 : x;
+                const float y = -x - dc;                  // Kahan: diag -= x (off-diagonal only)
                 const float s = diag + y;
-                dc = (s - diag) - y;
-                diag = s;
+                const float c = (s - diag) - y;
+                diag = dj ? diag : s;
+                dc = dj ? dc : c;
             }
 #pragma unroll
-            for (int j = 0; j < K; j++)
-                if (j == i) row[j] = diag;
+            for (int j = 0; j < K; j++) row[j] = (j == i) ? diag : row[j];
             const double rs = rowsum_minus_one(m, md, i, exs[bsel]);
             if (neg) status_min(status_key + r, b, i, PCSF_ENEGP);
             else if (fabs(rs) > m.tol) status_min(status_key + r, b, i, PCSF_EROWSUM);
