@@ -36,16 +36,67 @@ __device__ __forceinline__ void mma_tf32(uint32_t dt, uint64_t ad, uint64_t bd, 
                  :: "r"(dt), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
 }
 
+// the same with the A operand in tensor memory (M = 128 rows on the 128 lanes, one
+// tf32 element per 32-bit column, K = 8 columns from address a_t)
+__device__ __forceinline__ void mma_tf32_ta(uint32_t dt, uint32_t a_t, uint64_t bd, uint32_t idesc, uint32_t acc)
+{
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                 " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n"
+                 :: "r"(dt), "r"(a_t), "l"(bd), "r"(idesc), "r"(acc));
+}
+
+// D (=|+=) A_lo B_hi + A_hi B_lo + A_hi B_hi over K = 64 (8 steps each, the small
+// products first): A 128 x 64 and B 64 x 64 tf32 in the K-major core-matrix layout,
+// hi halves at sA / sB, lo halves a_lo / b_lo bytes further.  The descriptors of step
+// k are the step-0 descriptors plus k steps (A 4096 B, B 2048 B, in 16-byte units),
+// so the issuing thread only adds: rebuilding them per MMA measured 1.5x slower.
+__device__ __forceinline__ void mma3_tf32(uint32_t dt, uint32_t sA, uint32_t a_lo, uint32_t sB, uint32_t b_lo,
+                                          uint32_t idesc, bool accumulate)
+{
+    const uint64_t dAhi = sdesc(sA, 2048, 128), dAlo = sdesc(sA + a_lo, 2048, 128);
+    const uint64_t dBhi = sdesc(sB, 1024, 128), dBlo = sdesc(sB + b_lo, 1024, 128);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        mma_tf32(dt, dAlo + 256 * k, dBhi + 128 * k, idesc, (accumulate || k > 0) ? 1u : 0u);
+        mma_tf32(dt, dAhi + 256 * k, dBlo + 128 * k, idesc, 1);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) mma_tf32(dt, dAhi + 256 * k, dBhi + 128 * k, idesc, 1);
+}
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
 {
     uint32_t r[16];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+    // load and wait in one asm block: no use of the values can be scheduled before the wait
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                 "tcgen05.wait::ld.sync.aligned;"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
                    "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-                 : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                 : "r"(taddr)
+                 : "memory");
 #pragma unroll
     for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]);
+}
+
+// two 16-column loads (each thread: its lane, columns a.. and b..) and one wait, in one
+// asm block so that no use of the values can be scheduled before the wait
+__device__ __forceinline__ void tmem_ld16x2(uint32_t ta, uint32_t tb, float *va, float *vb)
+{
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n"
+                 "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n"
+                 "tcgen05.wait::ld.sync.aligned;"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+                   "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+                   "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(ta), "r"(tb)
+                 : "memory");
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        va[j] = __uint_as_float(r[j]);
+        vb[j] = __uint_as_float(r[16 + j]);
+    }
 }
 
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float *v)

@@ -79,14 +79,7 @@ __device__ __forceinline__ void td_store_a(unsigned char *sm, int site, int s0, 
 
 __device__ __forceinline__ void td_mma3(uint32_t dt, uint32_t sA, uint32_t sB, uint32_t idesc)
 {
-    uint32_t acc = 0;
-    for (int k = 0; k < 8; k++) {
-        mma_tf32(dt, sdesc(sA + TD_ABYTES + k * 4096, 2048, 128), sdesc(sB + k * 2048, 1024, 128), idesc, acc);
-        acc = 1;
-        mma_tf32(dt, sdesc(sA + k * 4096, 2048, 128), sdesc(sB + TD_BBYTES + k * 2048, 1024, 128), idesc, 1);
-    }
-    for (int k = 0; k < 8; k++)
-        mma_tf32(dt, sdesc(sA + k * 4096, 2048, 128), sdesc(sB + k * 2048, 1024, 128), idesc, 1);
+    mma3_tf32(dt, sA, TD_ABYTES, sB, TD_BBYTES, idesc, false);
 }
 
 __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, const float *Qop, const double *branch,

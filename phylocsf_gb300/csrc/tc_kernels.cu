@@ -15,11 +15,20 @@
 //
 // Layout: 256 threads; thread t owns tile column (site) t % 128, i.e. TMEM lane
 // t % 128, and states 32*(t/128) .. +31 (warp w reaches lanes 32*(w%4)..).
-// Tensor memory holds only the partial slots (64 columns each).  A child's
-// partial alpha_c is copied into the A operand (shared memory, hi and lo parts,
-// from which alpha_c = hi + lo exactly), so the MMA writes D_c over the child's
-// own slot; the epilogue reads alpha_c back from the A operand.  With
-// nslots * 64 <= 256 columns two CTAs share an SM.
+// Tensor memory holds the partial slots as regions of 64 columns (at least four:
+// 256 columns, so two CTAs share an SM).  A contraction has two forms:
+//  - region form (a tensor-memory region holds no live partial): the hi part of
+//    alpha_c is written back over the child's own slot and is the MMA's A operand
+//    there, the lo part goes to shared memory, and D goes to the free region;
+//  - shared form (every region is live, e.g. 6 of the 56 contractions of the
+//    58-leaf tree): hi and lo both go to the shared-memory A operand and D is
+//    written over the child's own slot.
+// The shared-memory data pipe is what bounds this kernel: the tensor cores' operand
+// reads share it with the threads' loads and stores.  The region form moves 80 KB
+// of operand reads per contraction instead of 144 KB, and 64 KB of thread traffic
+// instead of 128 KB.  Both forms issue the same MMAs in the same order on the same
+// values, so their results are identical.  The epilogue reads alpha_c = hi + lo
+// back from where the staging put them.
 //
 // Shared memory (about 106 KB for 58 leaves): one A operand (128 x 64, hi + lo),
 // one B operand (64 x 64, hi + lo), the tile's leaf states and the schedule.
@@ -58,8 +67,11 @@ constexpr int TCP_MAX_LEAVES = 160;
 // dynamic shared-memory map (bytes)
 constexpr uint32_t SM_A = 0;            // [hi, lo][128 x 64 fp32] = 2 x 32 KB
 constexpr uint32_t SM_B = 65536;        // [hi, lo][64 x 64 fp32]  = 2 x 16 KB
-constexpr uint32_t SM_LV = 98304;       // [nl][128] leaf states, then the schedule
+constexpr uint32_t SM_LV = 98304;       // [nl][LV_STRIDE] leaf states, then the schedule
 constexpr uint32_t A_BYTES = 32768, B_BYTES = 16384;
+// leaf-state rows padded by 4 bytes: the tile fill writes one byte per (site, leaf)
+// with consecutive threads on consecutive leaves, which would otherwise all hit one bank
+constexpr int LV_STRIDE = TCP_M + 4;
 
 
 // alpha = hi + lo of this thread's 32 states, read back from the A operand
@@ -86,6 +98,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
     __shared__ float cmax[2][2][TCP_M];
     __shared__ double red_l[TCP_THREADS / 32], red_e[TCP_THREADS / 32];
     __shared__ int16_t bseq[TCP_MAX_LEAVES];     // internal children in contraction order
+    __shared__ int8_t dreg[TCP_MAX_LEAVES];      // per contraction: free region for D, or -1
     __shared__ int nbseq_s;
 
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -94,7 +107,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
     const int s0 = 32 * half;
     const int nl = a.nl;
     uint8_t *lvT = sm + SM_LV;
-    SchedNode *sched = reinterpret_cast<SchedNode *>(sm + SM_LV + ((nl * TCP_M + 15) & ~15));
+    SchedNode *sched = reinterpret_cast<SchedNode *>(sm + SM_LV + ((nl * LV_STRIDE + 15) & ~15));
     const uint32_t barM = smem_addr(&bar_mma), barB = smem_addr(&bar_b);
     const uint32_t sA = smem_addr(sm + SM_A), sB = smem_addr(sm + SM_B);
     // kind::tf32, D f32, A/B tf32, both K-major, N = 64, M = 128
@@ -110,11 +123,23 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(barM), "r"(1));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(barB), "r"(1));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // replay the schedule's slot occupancy: a contraction takes the region form
+        // when some region holds no live partial (the contracted child's slot stays
+        // live until its epilogue has read it)
+        const uint32_t all = (tmem_cols >= 512) ? 0xFFu : ((1u << (tmem_cols / 64)) - 1u);
+        uint32_t occ = 0;
         int k = 0;
         for (int f = 0; f < a.n_internal; f++) {
             const SchedNode sn = a.sched[f];
-            if (sn.lslot >= 0) bseq[k++] = sn.lc;
-            if (sn.rslot >= 0) bseq[k++] = sn.rc;
+            for (int side = 0; side < 2; side++) {
+                const int s = side ? sn.rslot : sn.lslot;
+                if (s < 0) continue;
+                const uint32_t fr = all & ~occ;
+                bseq[k] = side ? sn.rc : sn.lc;
+                dreg[k++] = fr ? (int8_t)(__ffs(fr) - 1) : (int8_t)-1;
+                occ &= ~(1u << s);
+            }
+            occ |= 1u << sn.oslot;
         }
         nbseq_s = k;
     }
@@ -141,23 +166,29 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
     };
     if (tid == 0) issue_next_b();
 
-    // stage alpha of slot s (this thread's 32 states) as the A operand, hi and lo
-    auto stage_a = [&](int s) {
+    // stage alpha of slot s (this thread's 32 states) as the A operand: lo to shared
+    // memory; hi to shared memory (shared form) or back over slot s (region form)
+    // (the output stores of earlier nodes are waited for here, before the first read)
+    auto stage_a = [&](int s, bool region) {
         const uint32_t ts = tbase + lane_off + 64 * s + s0;
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        float x[32];
+        tmem_ld16x2(ts, ts + 16, x, x + 16);
 #pragma unroll
-        for (int q = 0; q < 2; q++) {
-            float x[16];
-            tmem_ld16(ts + 16 * q, x);
-#pragma unroll
-            for (int j4 = 0; j4 < 4; j4++) {
-                const float4 hv = make_float4(tf32_hi(x[4 * j4]), tf32_hi(x[4 * j4 + 1]), tf32_hi(x[4 * j4 + 2]),
-                                              tf32_hi(x[4 * j4 + 3]));
-                const float4 lv = make_float4(x[4 * j4] - hv.x, x[4 * j4 + 1] - hv.y, x[4 * j4 + 2] - hv.z,
-                                              x[4 * j4 + 3] - hv.w);
-                const uint32_t o = core_off(site, s0 + 16 * q + 4 * j4, 16);
-                *reinterpret_cast<float4 *>(sm + SM_A + o) = hv;
-                *reinterpret_cast<float4 *>(sm + SM_A + A_BYTES + o) = lv;
-            }
+        for (int j4 = 0; j4 < 8; j4++) {
+            const float4 hv = make_float4(tf32_hi(x[4 * j4]), tf32_hi(x[4 * j4 + 1]), tf32_hi(x[4 * j4 + 2]),
+                                          tf32_hi(x[4 * j4 + 3]));
+            const float4 lv = make_float4(x[4 * j4] - hv.x, x[4 * j4 + 1] - hv.y, x[4 * j4 + 2] - hv.z,
+                                          x[4 * j4 + 3] - hv.w);
+            const uint32_t o = core_off(site, s0 + 4 * j4, 16);
+            if (!region) *reinterpret_cast<float4 *>(sm + SM_A + o) = hv;
+            *reinterpret_cast<float4 *>(sm + SM_A + A_BYTES + o) = lv;
+            x[4 * j4] = hv.x; x[4 * j4 + 1] = hv.y; x[4 * j4 + 2] = hv.z; x[4 * j4 + 3] = hv.w;
+        }
+        if (region) {
+            tmem_st16(ts, x);
+            tmem_st16(ts + 16, x + 16);
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     };
@@ -168,32 +199,62 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
         b_inflight--;
         return true;
     };
-    // thread 0, after the staging barrier: D (slot s) = A B
-    auto issue_mma = [&](int s) {
-        const uint32_t dt = tbase + 64 * s;
-        uint32_t acc = 0;
-        if (NPROD == 3) {
-            for (int k = 0; k < 8; k++) {
-                mma_tf32(dt, sdesc(sA + A_BYTES + k * 4096, 2048, 128), sdesc(sB + k * 2048, 1024, 128), idesc, acc);
-                acc = 1;
-                mma_tf32(dt, sdesc(sA + k * 4096, 2048, 128), sdesc(sB + B_BYTES + k * 2048, 1024, 128), idesc, 1);
+    // thread 0, after the staging barrier: D = A B into region r (region form: A hi in
+    // slot s) or over slot s (shared form, r < 0); the same MMA sequence either way
+    // Descriptors of K-step k are the step-0 descriptors plus k times the step in
+    // 16-byte units (A 4096 B, B 2048 B), so the issuing loop is adds only.
+    const uint64_t dAhi = sdesc(sA, 2048, 128), dAlo = sdesc(sA + A_BYTES, 2048, 128);
+    const uint64_t dBhi = sdesc(sB, 1024, 128), dBlo = sdesc(sB + B_BYTES, 1024, 128);
+    auto issue_mma = [&](int s, int r) {
+        const uint32_t dt = tbase + 64 * (r >= 0 ? r : s);
+        const uint32_t ta = tbase + 64 * s;
+        if (r >= 0) {
+            if (NPROD == 3) {
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    mma_tf32(dt, dAlo + 256 * k, dBhi + 128 * k, idesc, k > 0);
+                    mma_tf32_ta(dt, ta + 8 * k, dBlo + 128 * k, idesc, 1);
+                }
             }
-        }
-        for (int k = 0; k < 8; k++) {
-            mma_tf32(dt, sdesc(sA + k * 4096, 2048, 128), sdesc(sB + k * 2048, 1024, 128), idesc, acc);
-            acc = 1;
+#pragma unroll
+            for (int k = 0; k < 8; k++) mma_tf32_ta(dt, ta + 8 * k, dBhi + 128 * k, idesc, NPROD == 3 || k > 0);
+        } else {
+            if (NPROD == 3) {
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    mma_tf32(dt, dAlo + 256 * k, dBhi + 128 * k, idesc, k > 0);
+                    mma_tf32(dt, dAhi + 256 * k, dBlo + 128 * k, idesc, 1);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 8; k++) mma_tf32(dt, dAhi + 256 * k, dBhi + 128 * k, idesc, NPROD == 3 || k > 0);
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                      :: "r"(barM) : "memory");
     };
-    // v (or v *=) alpha + D for the internal child in slot s; A operand still holds alpha
-    auto child_value = [&](int s, float *v, bool mul) {
-        const uint32_t tD = tbase + lane_off + 64 * s + s0;
+    // v (or v *=) alpha + D for the internal child in slot s, alpha = hi + lo from
+    // where stage_a put them
+    auto child_value = [&](int s, int r, float *v, bool mul) {
+        const uint32_t tD = tbase + lane_off + 64 * (r >= 0 ? r : s) + s0;
+        const uint32_t tH = tbase + lane_off + 64 * s + s0;
 #pragma unroll
         for (int q = 0; q < 2; q++) {
             float d[16], x[16];
-            tmem_ld16(tD + 16 * q, d);
-            load_alpha(sm, site, s0, q, x);
+            if (r >= 0) {
+                tmem_ld16x2(tD + 16 * q, tH + 16 * q, d, x);
+#pragma unroll
+                for (int j4 = 0; j4 < 4; j4++) {
+                    const float4 l = *reinterpret_cast<const float4 *>(
+                        sm + SM_A + A_BYTES + core_off(site, s0 + 16 * q + 4 * j4, 16));
+                    x[4 * j4 + 0] += l.x;
+                    x[4 * j4 + 1] += l.y;
+                    x[4 * j4 + 2] += l.z;
+                    x[4 * j4 + 3] += l.w;
+                }
+            } else {
+                tmem_ld16(tD + 16 * q, d);
+                load_alpha(sm, site, s0, q, x);
+            }
 #pragma unroll
             for (int j = 0; j < 16; j++) {
                 const float u = x[j] + d[j];
@@ -220,6 +281,20 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
             for (int k = 0; k < 4; k++) v[4 * j4 + k] = mul ? v[4 * j4 + k] * u[k] : u[k];
         }
     };
+    // the leaf beside an internal child in two steps: raw E^T row, then the identity
+    // part (or 1 where marginalised)
+    auto leaf_load = [&](const float *Pc, int s, float *v) {
+        const float4 *row = reinterpret_cast<const float4 *>(Pc + (size_t)(s < K ? s : 0) * K + s0);
+#pragma unroll
+        for (int j4 = 0; j4 < 8; j4++) {
+            const float4 x = __ldg(row + j4);
+            v[4 * j4] = x.x; v[4 * j4 + 1] = x.y; v[4 * j4 + 2] = x.z; v[4 * j4 + 3] = x.w;
+        }
+    };
+    auto leaf_fix = [&](int s, float *v) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) v[j] = (s < K) ? v[j] + ((s == s0 + j) ? 1.0f : 0.0f) : 1.0f;
+    };
 
     for (int w = blockIdx.x; w < a.nwi && ok; w += gridDim.x) {
         const WorkItem wi = a.wi[w];
@@ -231,52 +306,52 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
         __syncthreads();
         for (int f = tid; f < TCP_M * nl; f += TCP_THREADS) {
             int c = f / nl, l = f - c * nl;
-            lvT[l * TCP_M + c] = (c < ncols) ? lg[f] : (uint8_t)K;
+            lvT[l * LV_STRIDE + c] = (c < ncols) ? lg[f] : (uint8_t)K;
         }
         __syncthreads();
         int escale = 0;     // this column's sum of rescale exponents
+        int kc = 0;         // contractions so far (index into bseq / dreg)
 
         for (int ni = 0; ni < a.n_internal && ok; ni++) {
             const SchedNode sn = sched[ni];
             float v[32];
-            // internal children are contracted one after the other (l before r);
-            // leaf children are gathered while the last contraction runs.  Every
-            // barrier also agrees on a timed-out wait (bad), so that all threads
-            // leave together.
+            // internal children are contracted one after the other (l before r); a
+            // leaf child beside an internal one is gathered while the MMAs run (loading
+            // it before the staging measured slower).  Every barrier also agrees on a
+            // timed-out wait (bad), so that all threads leave together.
             const int slotL = sn.lslot, slotR = sn.rslot;
             const int nint = (slotL >= 0) + (slotR >= 0);
-            bool have = false, bad = false;
+            const int lfc = (slotL < 0) ? sn.lc : sn.rc;   // the leaf child when nint == 1
+            bool have = (nint == 1), bad = false;
+            int nc = 0;
             for (int side = 0; side < 2; side++) {
                 const int s = side ? slotR : slotL;
                 if (s < 0) continue;
-                if (have && __syncthreads_or(bad)) { ok = false; break; }   // the A operand is free again
-                stage_a(s);
+                if (nc++ && __syncthreads_or(bad)) { ok = false; break; }   // the A operand is free again
+                const int r = dreg[kc++];
+                stage_a(s, r >= 0);
                 if (tid == 0 && !wait_b()) bad = true;
                 tc_fence_before();
                 if (__syncthreads_or(bad)) { ok = false; break; }
                 tc_fence_after();
-                if (tid == 0) issue_mma(s);
-                const bool last = (nint == 1) || side == 1;
-                if (last) {
-                    for (int ls = 0; ls < 2; ls++) {
-                        if ((ls ? slotR : slotL) >= 0) continue;
-                        const int c = ls ? sn.rc : sn.lc;
-                        leaf_value(Pbase + (size_t)c * K2, lvT[c * TCP_M + site], v, have);
-                        have = true;
-                    }
+                if (tid == 0) issue_mma(s, r);
+                if (nint == 1) {
+                    const int ls = lvT[lfc * LV_STRIDE + site];
+                    leaf_load(Pbase + (size_t)lfc * K2, ls, v);
+                    leaf_fix(ls, v);
                 }
                 const bool done = mbar_wait(barM, ph_mma);
                 ph_mma ^= 1u;
                 tc_fence_after();
                 if (!done) bad = true;
                 if (tid == 0 && done) issue_next_b();     // the B operand is free again
-                child_value(s, v, have);
+                child_value(s, r, v, have);
                 have = true;
             }
             if (!ok) break;
             if (nint == 0) {
-                leaf_value(Pbase + (size_t)sn.lc * K2, lvT[sn.lc * TCP_M + site], v, false);
-                leaf_value(Pbase + (size_t)sn.rc * K2, lvT[sn.rc * TCP_M + site], v, true);
+                leaf_value(Pbase + (size_t)sn.lc * K2, lvT[sn.lc * LV_STRIDE + site], v, false);
+                leaf_value(Pbase + (size_t)sn.rc * K2, lvT[sn.rc * LV_STRIDE + site], v, true);
             }
             // ---- rescale by an exact power of two and park in the output slot
             float mx = 0.0f;
@@ -296,7 +371,6 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
                 for (int j = 0; j < 16; j++) y[j] = scale2(v[16 * q + j], -e);
                 tmem_st16(tO + 16 * q, y);
             }
-            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         }
         if (!ok) break;
         // ---- root: z = alpha_root . prior, elpr term, FP64 sums over the tile
@@ -307,6 +381,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
             const double *pr = a.m.prior + md * K + s0;
             const double *wl = a.m.wlog + md * K + s0;
             double z = 0.0, wz = 0.0;
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");   // the root's output store
 #pragma unroll
             for (int q = 0; q < 2; q++) {
                 float x[16];
@@ -358,6 +433,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
         }
     }
     if (!ok) mbar_wait(barM, ph_mma);
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -367,14 +443,15 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
 
 static uint32_t tmem_cols_for(int nslots)
 {
-    uint32_t need = (uint32_t)(64 * (nslots > 0 ? nslots : 1)), c = 32;
+    // at least four regions, so that most contractions find a free one for D
+    uint32_t need = (uint32_t)(64 * (nslots > 0 ? nslots : 1)), c = 256;
     while (c < need) c <<= 1;
     return c;
 }
 
 size_t prune_tc_smem_bytes(int nl, int nint)
 {
-    return SM_LV + (((size_t)nl * TCP_M + 15) & ~(size_t)15) + (size_t)nint * sizeof(SchedNode);
+    return SM_LV + (((size_t)nl * LV_STRIDE + 15) & ~(size_t)15) + (size_t)nint * sizeof(SchedNode);
 }
 
 bool prune_tc_supported(int nslots, int nl) { return nslots <= TCP_MAX_SLOTS && nl <= TCP_MAX_LEAVES; }

@@ -146,14 +146,7 @@ __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const 
         __syncthreads();
         tc_fence_after();
         if (tid == 0) {
-            uint32_t acc = 0;
-            for (int k = 0; k < 8; k++) {
-                mma_tf32(tbase, sdesc(sA + 32768 + k * 4096, 2048, 128), sdesc(sB + k * 2048, 1024, 128), idesc, acc);
-                acc = 1;
-                mma_tf32(tbase, sdesc(sA + k * 4096, 2048, 128), sdesc(sB + 16384 + k * 2048, 1024, 128), idesc, 1);
-            }
-            for (int k = 0; k < 8; k++)
-                mma_tf32(tbase, sdesc(sA + k * 4096, 2048, 128), sdesc(sB + k * 2048, 1024, 128), idesc, 1);
+            mma3_tf32(tbase, sA, 32768, sB, 16384, idesc, false);
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                          :: "r"(barM) : "memory");
         }
