@@ -133,6 +133,16 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
 // MMA drops (it reads 10 mantissa bits) cancel on average instead of always shrinking |x|
 __device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u); }
 
+// eight consecutive floats from read-only global memory in one 256-bit load (the address
+// 32-byte aligned): a warp gathering 32 rows then reads each 32-byte sector once instead
+// of twice with two 128-bit loads
+__device__ __forceinline__ void ldg8(const float *p, float *r)
+{
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(r[0]), "=f"(r[1]), "=f"(r[2]), "=f"(r[3]), "=f"(r[4]), "=f"(r[5]), "=f"(r[6]), "=f"(r[7])
+        : "l"(p));
+}
+
 // one bulk copy global -> shared of `bytes` (a multiple of 16, both addresses
 // 16-byte aligned), completing on mbarrier bar, which expects those bytes
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar)

@@ -182,19 +182,14 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
     // leaf child c: P_c[:, s] for this thread's states (1 for a marginalised leaf)
     auto leaf_col = [&](const float *Pbase, int c, float *v) {
         const int st = lvT[c * TD_M + site];
-        const float4 *row = reinterpret_cast<const float4 *>(Pbase + (size_t)c * K2 + (size_t)(st < K ? st : 0) * K + s0);
+        const float *row = Pbase + (size_t)c * K2 + (size_t)(st < K ? st : 0) * K + s0;
 #pragma unroll
-        for (int j4 = 0; j4 < TD_NS / 4; j4++) {
-            float4 x = make_float4(1.f, 1.f, 1.f, 1.f);
-            if (st < K) {
-                x = __ldg(row + j4);
-                const int a0 = s0 + 4 * j4;
-                x.x += (st == a0) ? 1.0f : 0.0f;
-                x.y += (st == a0 + 1) ? 1.0f : 0.0f;
-                x.z += (st == a0 + 2) ? 1.0f : 0.0f;
-                x.w += (st == a0 + 3) ? 1.0f : 0.0f;
-            }
-            v[4 * j4] = x.x; v[4 * j4 + 1] = x.y; v[4 * j4 + 2] = x.z; v[4 * j4 + 3] = x.w;
+        for (int j8 = 0; j8 < TD_NS / 8; j8++) {
+            float x[8];
+            ldg8(row + 8 * j8, x);
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                v[8 * j8 + k] = (st < K) ? x[k] + ((st == s0 + 8 * j8 + k) ? 1.0f : 0.0f) : 1.0f;
         }
     };
     // x = A (hi + lo) + D(cols)

@@ -264,32 +264,24 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
     };
     // leaf child: v (or v *=) P_c[a][s] = E^T[s][a] + (a == s), 1 if marginalised
     auto leaf_value = [&](const float *Pc, int s, float *v, bool mul) {
-        const float4 *row = reinterpret_cast<const float4 *>(Pc + (size_t)(s < K ? s : 0) * K + s0);
+        const float *row = Pc + (size_t)(s < K ? s : 0) * K + s0;
 #pragma unroll
-        for (int j4 = 0; j4 < 8; j4++) {
-            float4 x = make_float4(1.f, 1.f, 1.f, 1.f);
-            if (s < K) {
-                x = __ldg(row + j4);
-                const int a0 = s0 + 4 * j4;
-                x.x += (s == a0) ? 1.0f : 0.0f;
-                x.y += (s == a0 + 1) ? 1.0f : 0.0f;
-                x.z += (s == a0 + 2) ? 1.0f : 0.0f;
-                x.w += (s == a0 + 3) ? 1.0f : 0.0f;
+        for (int j8 = 0; j8 < 4; j8++) {
+            float x[8];
+            ldg8(row + 8 * j8, x);
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const float u = (s < K) ? x[k] + ((s == s0 + 8 * j8 + k) ? 1.0f : 0.0f) : 1.0f;
+                v[8 * j8 + k] = mul ? v[8 * j8 + k] * u : u;
             }
-            const float u[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-            for (int k = 0; k < 4; k++) v[4 * j4 + k] = mul ? v[4 * j4 + k] * u[k] : u[k];
         }
     };
     // the leaf beside an internal child in two steps: raw E^T row, then the identity
     // part (or 1 where marginalised)
     auto leaf_load = [&](const float *Pc, int s, float *v) {
-        const float4 *row = reinterpret_cast<const float4 *>(Pc + (size_t)(s < K ? s : 0) * K + s0);
+        const float *row = Pc + (size_t)(s < K ? s : 0) * K + s0;
 #pragma unroll
-        for (int j4 = 0; j4 < 8; j4++) {
-            const float4 x = __ldg(row + j4);
-            v[4 * j4] = x.x; v[4 * j4 + 1] = x.y; v[4 * j4 + 2] = x.z; v[4 * j4 + 3] = x.w;
-        }
+        for (int j8 = 0; j8 < 4; j8++) ldg8(row + 8 * j8, v + 8 * j8);
     };
     auto leaf_fix = [&](int s, float *v) {
 #pragma unroll
