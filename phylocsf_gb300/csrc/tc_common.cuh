@@ -64,6 +64,22 @@ __device__ __forceinline__ void mma3_tf32(uint32_t dt, uint32_t sA, uint32_t a_l
     for (int k = 0; k < 8; k++) mma_tf32(dt, dAhi + 256 * k, dBhi + 128 * k, idesc, 1);
 }
 
+// the same products with A_hi in tensor memory (64 columns from ta_hi, lane r = row r)
+// and A_lo in shared memory at sAlo: same MMA order, so the same D
+__device__ __forceinline__ void mma3_tf32_ta(uint32_t dt, uint32_t ta_hi, uint32_t sAlo, uint32_t sB, uint32_t b_lo,
+                                             uint32_t idesc)
+{
+    const uint64_t dAlo = sdesc(sAlo, 2048, 128);
+    const uint64_t dBhi = sdesc(sB, 1024, 128), dBlo = sdesc(sB + b_lo, 1024, 128);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        mma_tf32(dt, dAlo + 256 * k, dBhi + 128 * k, idesc, k > 0 ? 1u : 0u);
+        mma_tf32_ta(dt, ta_hi + 8 * k, dBlo + 128 * k, idesc, 1);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) mma_tf32_ta(dt, ta_hi + 8 * k, dBhi + 128 * k, idesc, 1);
+}
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
 {
     uint32_t r[16];

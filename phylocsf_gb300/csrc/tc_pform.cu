@@ -16,8 +16,10 @@
 // leaves (row gathers) and the pre-split B operand for the branches above
 // internal nodes.
 //
-// One CTA (128 threads, ~98 KB shared memory, 64 tensor-memory columns) per P
-// set walks its branch pairs.  mbarrier waits are bounded as in the pruning
+// One CTA (128 threads) per P set walks its branch pairs.  A_hi sits in tensor
+// memory (columns 64..127, lane r = row r) and only A_lo in shared memory, so a CTA
+// takes 64 KB of shared memory and 128 tensor-memory columns and three CTAs share an
+// SM (the kernel is bound by the latency of its per-pair chain).  mbarrier waits are bounded as in the pruning
 // kernel; on timeout the CTA records an error, waits (bounded) for its MMAs,
 // frees its tensor memory and stops.
 #include <cmath>
@@ -31,9 +33,9 @@ namespace pcsf {
 
 constexpr int PFT_THREADS = 128;
 constexpr uint32_t PFT_B = 0;          // [hi, lo][64 x 64]   B = U^T D^1/2, 2 x 16 KB
-constexpr uint32_t PFT_A = 32768;      // [hi, lo][128 x 64]  A, 2 x 32 KB
-constexpr uint32_t PFT_SMEM = 98304;
-constexpr uint32_t PFT_TMEM_COLS = 64;
+constexpr uint32_t PFT_A = 32768;      // [128 x 64]  A_lo, 32 KB
+constexpr uint32_t PFT_SMEM = 65536;
+constexpr uint32_t PFT_TMEM_COLS = 128;   // D in 0..63, A_hi in 64..127
 constexpr int PFT_MAX_BRANCHES = 320;
 
 __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const double *branch, int nbr, int nl,
@@ -126,27 +128,33 @@ __global__ void __launch_bounds__(PFT_THREADS) k_pform_tc(const PSet *ps, const 
             exs[bsel][i] = listed ? (double)expm1f(lam_i * t) : 0.0;
         }
         __syncthreads();
-        // ---- A operand: row tid = isq_i U_im cf_m, TF32 hi / lo
+        // ---- A operand: row tid = isq_i U_im cf_m, TF32 hi (tensor memory) / lo (shared)
         {
             const float4 *urow = reinterpret_cast<const float4 *>(Uf + (size_t)i * K);
-#pragma unroll 4
-            for (int q = 0; q < K / 4; q++) {
-                const float4 u = __ldg(urow + q);
-                const float x0 = isq_i * u.x * cfs[bsel][4 * q], x1 = isq_i * u.y * cfs[bsel][4 * q + 1];
-                const float x2 = isq_i * u.z * cfs[bsel][4 * q + 2], x3 = isq_i * u.w * cfs[bsel][4 * q + 3];
-                const float4 hv = make_float4(tf32_hi(x0), tf32_hi(x1), tf32_hi(x2), tf32_hi(x3));
-                const uint32_t o = core_off(tid, 4 * q, 16);
-                *reinterpret_cast<float4 *>(sm + PFT_A + o) = hv;
-                *reinterpret_cast<float4 *>(sm + PFT_A + 32768 + o) = make_float4(x0 - hv.x, x1 - hv.y, x2 - hv.z,
-                                                                                  x3 - hv.w);
+#pragma unroll 1
+            for (int c = 0; c < 4; c++) {
+                float h[16];
+#pragma unroll
+                for (int q4 = 0; q4 < 4; q4++) {
+                    const int q = 4 * c + q4;
+                    const float4 u = __ldg(urow + q);
+                    const float x0 = isq_i * u.x * cfs[bsel][4 * q], x1 = isq_i * u.y * cfs[bsel][4 * q + 1];
+                    const float x2 = isq_i * u.z * cfs[bsel][4 * q + 2], x3 = isq_i * u.w * cfs[bsel][4 * q + 3];
+                    const float4 hv = make_float4(tf32_hi(x0), tf32_hi(x1), tf32_hi(x2), tf32_hi(x3));
+                    *reinterpret_cast<float4 *>(sm + PFT_A + core_off(tid, 4 * q, 16)) =
+                        make_float4(x0 - hv.x, x1 - hv.y, x2 - hv.z, x3 - hv.w);
+                    h[4 * q4] = hv.x; h[4 * q4 + 1] = hv.y; h[4 * q4 + 2] = hv.z; h[4 * q4 + 3] = hv.w;
+                }
+                tmem_st16(tbase + lane_off + 64 + 16 * c, h);
             }
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
         if (tid == 0) {
-            mma3_tf32(tbase, sA, 32768, sB, 16384, idesc, false);
+            mma3_tf32_ta(tbase, tbase + 64, sA, sB, 16384, idesc);
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                          :: "r"(barM) : "memory");
         }
