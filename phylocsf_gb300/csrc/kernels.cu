@@ -466,6 +466,22 @@ __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
         const T *Pbase = reinterpret_cast<const T *>(a.Pbuf) + (size_t)rq.pset * a.nbr * K2;
         const int ncols = wi.ncols;
         const uint8_t *lg = a.leaves + (size_t)wi.col0 * nl;
+        // E^T of a node's internal children into shared memory, copied asynchronously one
+        // node ahead (issued once the previous node's contraction has released the
+        // buffers); leaf children read their rows from global memory instead
+        auto copy_inner = [&](const SchedNode &nx) {
+            constexpr int NV = K2 * sizeof(T) / 16;
+#pragma unroll
+            for (int side = 0; side < 2; side++) {
+                if ((side ? nx.rslot : nx.lslot) < 0) continue;
+                const char *src = reinterpret_cast<const char *>(Pbase + (size_t)(side ? nx.rc : nx.lc) * K2);
+                const uint32_t dst = (uint32_t)__cvta_generic_to_shared(Et + side * K2);
+                for (int f = tid; f < NV; f += PR_THREADS)
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(dst + 16 * f), "l"(src + 16 * f)
+                                 : "memory");
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
+        };
         __syncthreads();   // previous work item finished with shared memory
         for (int f = tid; f < TC * nl; f += PR_THREADS) {
             int c = f / nl, l = f - c * nl;
@@ -485,24 +501,17 @@ __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
             }
         }
 
+        copy_inner(sched[0]);
         for (int ni = 0; ni < a.n_internal; ni++) {
             const SchedNode sn = sched[ni];
-            {
-                const float4 *gl = reinterpret_cast<const float4 *>(Pbase + (size_t)sn.lc * K2);
-                const float4 *gr = reinterpret_cast<const float4 *>(Pbase + (size_t)sn.rc * K2);
-                float4 *sl = reinterpret_cast<float4 *>(Et);
-                float4 *sr = reinterpret_cast<float4 *>(Et + K2);
-                constexpr int NV = K2 * sizeof(T) / 16;
-                for (int f = tid; f < NV; f += PR_THREADS) {
-                    sl[f] = __ldg(gl + f);
-                    sr[f] = __ldg(gr + f);
-                }
-            }
+            asm volatile("cp.async.wait_all;" ::: "memory");
             __syncthreads();
             T vl[4][CPT], vr[4][CPT];
-            child_partial<T, TC, KAHAN>(Et, slots, sn.lslot, sn.lc, lvT, a0, c0, vl, dcol0);
-            child_partial<T, TC, KAHAN>(Et + K2, slots, sn.rslot, sn.rc, lvT, a0, c0, vr, dcol0);
+            child_partial<T, TC, KAHAN>(Et, slots, sn.lslot, sn.lc, lvT, a0, c0, vl, dcol0, Pbase + (size_t)sn.lc * K2);
+            child_partial<T, TC, KAHAN>(Et + K2, slots, sn.rslot, sn.rc, lvT, a0, c0, vr, dcol0,
+                                        Pbase + (size_t)sn.rc * K2);
             __syncthreads();
+            if (ni + 1 < a.n_internal) copy_inner(sched[ni + 1]);   // E^T buffers are free again
             MU *cm = colmax + (ni & 1) * TC;
             MU *cm_next = colmax + ((ni + 1) & 1) * TC;
             if (tid < TC) cm_next[tid] = 0;

@@ -229,10 +229,26 @@ __device__ inline void contract(const T *M, const T *X, int a0, int c0, T out[4]
 // leaf in state s (1 for a marginalised leaf: P rows sum to 1).
 template <typename T, int TC, int KAHAN>
 __device__ inline void child_partial(const T *Et, const T *slots, int slot, int leaf, const uint8_t *lvT, int a0,
-                                     int c0, T v[4][TC / 16], int64_t dither_col0 = -1)
+                                     int c0, T v[4][TC / 16], int64_t dither_col0 = -1, const T *leaf_g = nullptr)
 {
     constexpr int CPT = TC / 16;
     if (slot < 0) {
+        if (leaf_g) {   // the leaf's E^T rows straight from global memory (4 states per column)
+#pragma unroll
+            for (int cc = 0; cc < CPT; cc++) {
+                const int s = lvT[leaf * TC + c0 + cc];
+                const T c = (dither_col0 >= 0) ? (T)(1.0f + (float)dither_k(dither_col0 + c0 + cc, leaf) * (1.0f / 256.0f))
+                                               : (T)1;
+                T e[4];
+                Vec4<T>::load(leaf_g + (size_t)(s < K ? s : 0) * K + a0, e);
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int a = a0 + i;
+                    v[i][cc] = (s >= K) ? c : fma(e[i], c, (a == s ? c : (T)0));
+                }
+            }
+            return;
+        }
 #pragma unroll
         for (int cc = 0; cc < CPT; cc++) {
             int s = lvT[leaf * TC + c0 + cc];
