@@ -46,6 +46,8 @@ constexpr uint32_t TD_BE = 65536;        // [hi, lo][64 x 64]     E_c, 2 x 16 KB
 constexpr uint32_t TD_BQ = 98304;        // [model][hi, lo][64 x 64]  Q, 2 x 2 x 16 KB
 constexpr uint32_t TD_LV = 163840;       // [nl][128] leaf states, then the schedule
 constexpr uint32_t TD_ABYTES = 32768, TD_BBYTES = 16384;
+// leaf-state rows padded by 4 bytes (the tile fill writes consecutive leaves from consecutive threads)
+constexpr int TD_LVS = TD_M + 4;
 
 __device__ __forceinline__ void td_load_alpha(const unsigned char *sm, int site, int s0, float *x)
 {
@@ -93,6 +95,7 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
     __shared__ int16_t bseq[TD_MAX_LEAVES];
     __shared__ float blen[2 * TD_MAX_LEAVES];     // branch lengths b_c (FP32)
     __shared__ int nbseq_s;
+    __shared__ float prf[K], wlf[K];             // this work item's model: prior, prior * log prior (FP32)
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int site = tid & (TD_M - 1);
@@ -100,7 +103,7 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
     const int s0 = TD_NS * quarter;
     const int nl = a.nl;
     uint8_t *lvT = sm + TD_LV;
-    SchedNode *sched = reinterpret_cast<SchedNode *>(sm + TD_LV + ((nl * TD_M + 15) & ~15));
+    SchedNode *sched = reinterpret_cast<SchedNode *>(sm + TD_LV + ((nl * TD_LVS + 15) & ~15));
     const uint32_t barM = smem_addr(&bar_mma), barB = smem_addr(&bar_b), barQ = smem_addr(&bar_q);
     const uint32_t sA = smem_addr(sm + TD_A), sBE = smem_addr(sm + TD_BE), sBQ = smem_addr(sm + TD_BQ);
     const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
@@ -181,7 +184,7 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
     };
     // leaf child c: P_c[:, s] for this thread's states (1 for a marginalised leaf)
     auto leaf_col = [&](const float *Pbase, int c, float *v) {
-        const int st = lvT[c * TD_M + site];
+        const int st = lvT[c * TD_LVS + site];
         const float *row = Pbase + (size_t)c * K2 + (size_t)(st < K ? st : 0) * K + s0;
 #pragma unroll
         for (int j8 = 0; j8 < TD_NS / 8; j8++) {
@@ -219,7 +222,11 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
         __syncthreads();
         for (int f = tid; f < TD_M * nl; f += TD_THREADS) {
             int c = f / nl, l = f - c * nl;
-            lvT[l * TD_M + c] = (c < ncols) ? lg[f] : (uint8_t)K;
+            lvT[l * TD_LVS + c] = (c < ncols) ? lg[f] : (uint8_t)K;
+        }
+        if (tid < K) {
+            prf[tid] = (float)a.m.prior[md * K + tid];
+            wlf[tid] = (float)a.m.wlog[md * K + tid];
         }
         __syncthreads();
         int escale = 0;
@@ -323,56 +330,66 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         }
         if (!ok) break;
-        // ---- root: z = pi . alpha, z' = pi . alpha', elpr term; FP64 per column
-        double *zpart = reinterpret_cast<double *>(sm + TD_A);   // [4][3][128]; the A operand is idle
+        // ---- root: z = pi . alpha, z' = pi . alpha', elpr term: FP32 compensated dot
+        // products, log z = log m + e ln 2 with m in [0.5, 1); FP64 for the per-column
+        // log and the sums over the tile only (as in k_prune_tc)
+        float *zpart = reinterpret_cast<float *>(sm + TD_A);   // [4][3][128]; the A operand is idle
         __syncthreads();
         {
             const uint32_t tR = tbase + lane_off + 128u * sched[a.n_internal - 1].oslot + s0;
-            const double *pr = a.m.prior + md * K + s0;
-            const double *wl = a.m.wlog + md * K + s0;
-            double z = 0.0, wz = 0.0, dz = 0.0;
+            float z = 0.0f, zc = 0.0f, wz = 0.0f, dz = 0.0f, dzc = 0.0f;
             float x[TD_NS], xd[TD_NS];
             tmem_ld16(tR, x);
             tmem_ld16(tR + 64, xd);
 #pragma unroll
             for (int j = 0; j < TD_NS; j++) {
-                z += (double)x[j] * pr[j];
-                wz += (double)x[j] * wl[j];
-                dz += (double)xd[j] * pr[j];
+                const float p = prf[s0 + j];
+                float y = x[j] * p - zc, t = z + y;
+                zc = (t - z) - y;
+                z = t;
+                y = xd[j] * p - dzc;
+                t = dz + y;
+                dzc = (t - dz) - y;
+                dz = t;
+                wz = fmaf(x[j], wlf[s0 + j], wz);
             }
             zpart[(quarter * 3 + 0) * TD_M + site] = z;
             zpart[(quarter * 3 + 1) * TD_M + site] = wz;
             zpart[(quarter * 3 + 2) * TD_M + site] = dz;
         }
         __syncthreads();
-        double tl = 0.0, te = 0.0, td = 0.0;
-        if (quarter == 0 && site < ncols) {
-            double z = 0.0, wz = 0.0, dz = 0.0;
-            for (int qq = 0; qq < 4; qq++) {     // fixed order
-                z += zpart[(qq * 3 + 0) * TD_M + site];
-                wz += zpart[(qq * 3 + 1) * TD_M + site];
-                dz += zpart[(qq * 3 + 2) * TD_M + site];
+        if (quarter == 0) {
+            double tl = 0.0, te = 0.0, td = 0.0;
+            if (site < ncols) {
+                float z = 0.0f, wz = 0.0f, dz = 0.0f;
+                for (int qq = 0; qq < 4; qq++) {     // fixed order
+                    z += zpart[(qq * 3 + 0) * TD_M + site];
+                    wz += zpart[(qq * 3 + 1) * TD_M + site];
+                    dz += zpart[(qq * 3 + 2) * TD_M + site];
+                }
+                if (z > 0.0f) {
+                    int ez;
+                    const float mz = frexpf(z, &ez);
+                    tl = (double)logf(mz) + (double)(ez + escale) * 0.69314718055994530942;
+                    te = (double)(wz / z);
+                    td = (double)(dz / z);
+                } else {
+                    tl = -INFINITY;
+                }
             }
-            if (z > 0.0) {
-                tl = log(z) + (double)escale * 0.69314718055994530942;
-                te = wz / z;
-                td = dz / z;
-            } else {
-                tl = -INFINITY;
-            }
-        }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            tl += __shfl_down_sync(0xffffffffu, tl, o);
-            te += __shfl_down_sync(0xffffffffu, te, o);
-            td += __shfl_down_sync(0xffffffffu, td, o);
+            for (int o = 16; o > 0; o >>= 1) {
+                tl += __shfl_down_sync(0xffffffffu, tl, o);
+                te += __shfl_down_sync(0xffffffffu, te, o);
+                td += __shfl_down_sync(0xffffffffu, td, o);
+            }
+            if ((tid & 31) == 0) { red[0][warp] = tl; red[1][warp] = te; red[2][warp] = td; }
         }
-        if ((tid & 31) == 0) { red[0][warp] = tl; red[1][warp] = te; red[2][warp] = td; }
         tc_fence_before();
         __syncthreads();
         if (tid == 0) {
             double sl = 0.0, se = 0.0, sd = 0.0;
-            for (int k = 0; k < TD_THREADS / 32; k++) { sl += red[0][k]; se += red[1][k]; sd += red[2][k]; }
+            for (int k = 0; k < TD_M / 32; k++) { sl += red[0][k]; se += red[1][k]; sd += red[2][k]; }
             a.partials[2 * (size_t)w] = sl;
             a.partials[2 * (size_t)w + 1] = se;
             dpart[2 * (size_t)w] = sd;
@@ -397,7 +414,7 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
 
 size_t prune_tc_dual_smem_bytes(int nl, int nint)
 {
-    return TD_LV + (((size_t)nl * TD_M + 15) & ~(size_t)15) + (size_t)nint * sizeof(SchedNode);
+    return TD_LV + (((size_t)nl * TD_LVS + 15) & ~(size_t)15) + (size_t)nint * sizeof(SchedNode);
 }
 
 bool prune_tc_dual_supported(int nslots, int nl) { return nslots <= TD_MAX_SLOTS && nl <= TD_MAX_LEAVES; }

@@ -100,6 +100,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
     __shared__ int16_t bseq[TCP_MAX_LEAVES];     // internal children in contraction order
     __shared__ int8_t dreg[TCP_MAX_LEAVES];      // per contraction: free region for D, or -1
     __shared__ int nbseq_s;
+    __shared__ float prf[K], wlf[K];             // this work item's model: prior, prior * log prior (FP32)
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int site = tid & (TCP_M - 1);          // tile column = TMEM lane
@@ -300,6 +301,10 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
             int c = f / nl, l = f - c * nl;
             lvT[l * LV_STRIDE + c] = (c < ncols) ? lg[f] : (uint8_t)K;
         }
+        if (tid < K) {
+            prf[tid] = (float)a.m.prior[md * K + tid];
+            wlf[tid] = (float)a.m.wlog[md * K + tid];
+        }
         __syncthreads();
         int escale = 0;     // this column's sum of rescale exponents
         int kc = 0;         // contractions so far (index into bseq / dreg)
@@ -365,14 +370,15 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
             }
         }
         if (!ok) break;
-        // ---- root: z = alpha_root . prior, elpr term, FP64 sums over the tile
-        double *zpart = reinterpret_cast<double *>(sm + SM_A);   // [2][2][128]; the A operand is idle here
+        // ---- root: z = alpha_root . prior (FP32, compensated) and the elpr term per column;
+        // log z = log m + e ln 2 with m in [0.5, 1) (logf of m is within ~4e-8 absolute,
+        // far below the tensor-core noise of these search values); FP64 only for the
+        // per-column log and the sums over the tile (this part's FP64 rate is ~1/64 of FP32)
+        float *zpart = reinterpret_cast<float *>(sm + SM_A);   // [2][2][128]; the A operand is idle here
         __syncthreads();
         {
             const uint32_t tR = tbase + lane_off + 64 * sched[a.n_internal - 1].oslot + s0;
-            const double *pr = a.m.prior + md * K + s0;
-            const double *wl = a.m.wlog + md * K + s0;
-            double z = 0.0, wz = 0.0;
+            float z = 0.0f, zc = 0.0f, wz = 0.0f;
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");   // the root's output store
 #pragma unroll
             for (int q = 0; q < 2; q++) {
@@ -380,36 +386,43 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
                 tmem_ld16(tR + 16 * q, x);
 #pragma unroll
                 for (int j = 0; j < 16; j++) {
-                    z += (double)x[j] * pr[16 * q + j];
-                    wz += (double)x[j] * wl[16 * q + j];
+                    const float y = x[j] * prf[s0 + 16 * q + j] - zc;
+                    const float t = z + y;
+                    zc = (t - z) - y;
+                    z = t;
+                    wz = fmaf(x[j], wlf[s0 + 16 * q + j], wz);
                 }
             }
             zpart[(half * 2 + 0) * TCP_M + site] = z;
             zpart[(half * 2 + 1) * TCP_M + site] = wz;
         }
         __syncthreads();
-        double tl = 0.0, te = 0.0;
-        if (half == 0 && site < ncols) {
-            const double z = zpart[0 * TCP_M + site] + zpart[2 * TCP_M + site];
-            const double wz = zpart[1 * TCP_M + site] + zpart[3 * TCP_M + site];
-            if (z > 0.0) {
-                tl = log(z) + (double)escale * 0.69314718055994530942;
-                te = wz / z;
-            } else {
-                tl = -INFINITY;
+        if (half == 0) {
+            double tl = 0.0, te = 0.0;
+            if (site < ncols) {
+                const float z = zpart[0 * TCP_M + site] + zpart[2 * TCP_M + site];
+                const float wz = zpart[1 * TCP_M + site] + zpart[3 * TCP_M + site];
+                if (z > 0.0f) {
+                    int ez;
+                    const float mz = frexpf(z, &ez);
+                    tl = (double)logf(mz) + (double)(ez + escale) * 0.69314718055994530942;
+                    te = (double)(wz / z);
+                } else {
+                    tl = -INFINITY;
+                }
             }
-        }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            tl += __shfl_down_sync(0xffffffffu, tl, o);
-            te += __shfl_down_sync(0xffffffffu, te, o);
+            for (int o = 16; o > 0; o >>= 1) {
+                tl += __shfl_down_sync(0xffffffffu, tl, o);
+                te += __shfl_down_sync(0xffffffffu, te, o);
+            }
+            if ((tid & 31) == 0) { red_l[warp] = tl; red_e[warp] = te; }
         }
-        if ((tid & 31) == 0) { red_l[warp] = tl; red_e[warp] = te; }
         tc_fence_before();
         __syncthreads();
         if (tid == 0) {
             double sl = 0.0, se = 0.0;
-            for (int k = 0; k < TCP_THREADS / 32; k++) { sl += red_l[k]; se += red_e[k]; }
+            for (int k = 0; k < TCP_M / 32; k++) { sl += red_l[k]; se += red_e[k]; }
             a.partials[2 * (size_t)w] = sl;
             a.partials[2 * (size_t)w + 1] = se;
         }
