@@ -163,6 +163,7 @@ struct pcsf_engine {
     int prune_grid = 0;
     int sm_count = 0;
     DevBuf<int> derr;     // set by a kernel whose bounded wait timed out
+    DevBuf<unsigned long long> dbadcode;   // first invalid leaf code of an uploaded batch
 
     pcsf_stats stats{};
 
@@ -2058,21 +2059,28 @@ int pcsf_batch_create(pcsf_engine *e, int32_t n_regions, const int64_t *col_offs
         return e->fail(PCSF_EINVAL, "pcsf_batch_create: leaves is NULL");
     }
     const size_t nbytes = (size_t)b->total_cols * e->nl;
-    for (size_t i = 0; i < nbytes; i++)
-        if (leaves[i] > PCSF_MARGINALIZE) {
-            size_t col = i / e->nl;
-            int lf = (int)(i % e->nl);
-            delete b;
-            return e->fail(PCSF_EINVAL, "pcsf_batch_create: leaf code %d at column %zu leaf %d (max %d)", leaves[i], col,
-                           lf, PCSF_MARGINALIZE);
-        }
+    // the codes are checked on the device after the upload (a host loop over a
+    // multi-GB batch would cost more than scoring it)
+    unsigned long long bad = ~0ull;
     cudaError_t ce = b->dleaves.reserve(nbytes + 16);
+    if (ce == cudaSuccess) ce = e->dbadcode.reserve(1);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(e->dbadcode.p, &bad, sizeof(bad), cudaMemcpyHostToDevice, e->stream);
     if (ce == cudaSuccess && nbytes)
         ce = cudaMemcpyAsync(b->dleaves.p, leaves, nbytes, cudaMemcpyHostToDevice, e->stream);
+    if (ce == cudaSuccess) ce = launch_check_codes(b->dleaves.p, nbytes, e->dbadcode.p, e->stream);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&bad, e->dbadcode.p, sizeof(bad), cudaMemcpyDeviceToHost, e->stream);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
     if (ce != cudaSuccess) {
         delete b;
         return e->cuda_fail(ce, "batch upload");
+    }
+    if (bad != ~0ull) {
+        const size_t col = (size_t)(bad / (unsigned long long)e->nl);
+        const int lf = (int)(bad % (unsigned long long)e->nl);
+        const int code = leaves[bad];
+        delete b;
+        return e->fail(PCSF_EINVAL, "pcsf_batch_create: leaf code %d at column %zu leaf %d (max %d)", code, col, lf,
+                       PCSF_MARGINALIZE);
     }
     *out = b;
     return PCSF_OK;

@@ -393,6 +393,40 @@ __global__ void __launch_bounds__(256) k_d2f_rows(const double *in, float *out, 
     }
 }
 
+// any byte of w above 64: (b & 0x7F) + 63 reaches bit 7 exactly when b & 0x7F > 64
+// (no carry between bytes: at most 190), and b's own bit 7 covers b >= 128
+__device__ __forceinline__ bool bytes_above_64(uint32_t w)
+{
+    return ((((w & 0x7F7F7F7Fu) + 0x3F3F3F3Fu) | w) & 0x80808080u) != 0u;
+}
+
+__global__ void k_check_codes(const uint8_t *codes, size_t n, unsigned long long *first_bad)
+{
+    const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    const size_t nv = n / 16;
+    for (size_t v = t0; v < nv; v += stride) {
+        const uint4 x = reinterpret_cast<const uint4 *>(codes)[v];
+        if (bytes_above_64(x.x) || bytes_above_64(x.y) || bytes_above_64(x.z) || bytes_above_64(x.w))
+            for (int j = 0; j < 16; j++)
+                if (codes[16 * v + j] > 64) {
+                    atomicMin(first_bad, (unsigned long long)(16 * v + j));
+                    break;
+                }
+    }
+    for (size_t i = 16 * nv + t0; i < n; i += stride)
+        if (codes[i] > 64) atomicMin(first_bad, (unsigned long long)i);
+}
+
+cudaError_t launch_check_codes(const uint8_t *codes, size_t n, unsigned long long *first_bad, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    size_t blocks = (n / 16 + 255) / 256;
+    if (blocks < 1) blocks = 1;
+    if (blocks > 4096) blocks = 4096;
+    k_check_codes<<<(unsigned)blocks, 256, 0, s>>>(codes, n, first_bad);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_d2f_rows(const double *in, float *out, size_t nmat, int nbr, float *bop, int bop_nl, cudaStream_t s)
 {
     if (nmat == 0) return cudaSuccess;

@@ -90,6 +90,9 @@ cudaError_t launch_pform(bool fp64, const PSet *ps, int nps, const double *branc
                          float *bop = nullptr, int bop_nl = 0);
 cudaError_t launch_d2f(const double *in, float *out, size_t n, cudaStream_t s);
 cudaError_t launch_d2f_rows(const double *in, float *out, size_t nmat, int nbr, float *bop, int bop_nl, cudaStream_t s);
+// Leaf codes of an uploaded batch: *first_bad = the smallest index of a byte > 64
+// (PCSF_MARGINALIZE), left unchanged when every code is valid.
+cudaError_t launch_check_codes(const uint8_t *codes, size_t n, unsigned long long *first_bad, cudaStream_t s);
 
 // Pruning over work items [nwi]; partials [nwi][2] (lpr, elpr).
 struct PruneArgs {
