@@ -164,6 +164,7 @@ struct pcsf_engine {
     int sm_count = 0;
     DevBuf<int> derr;     // set by a kernel whose bounded wait timed out
     DevBuf<unsigned long long> dbadcode;   // first invalid leaf code of an uploaded batch
+    DevBuf<float> Dlo;    // [chunk P sets][nbr][K] low parts of diag(E) (SIMT FP32 evaluations)
 
     pcsf_stats stats{};
 
@@ -714,6 +715,10 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     for (size_t c = 0; c + 1 < chunk_ps_begin.size(); c++)
         max_chunk_ps = std::max<size_t>(max_chunk_ps, chunk_ps_begin[c + 1] - chunk_ps_begin[c]);
     CK(e->Pbuf.reserve(max_chunk_ps * pset_bytes), "cudaMalloc P(t) buffer");
+    // low parts of diag(E) for the SIMT FP32 kernel (not for the tensor-core search)
+    const bool want_dlo = e->prec != PCSF_PREC_FP64 && !tc && !grad;
+    if (want_dlo) CK(e->Dlo.reserve(max_chunk_ps * (size_t)e->nbr * K), "cudaMalloc P(t) diagonal buffer");
+    float *dlo = want_dlo ? e->Dlo.p : nullptr;
     const bool stage64 = (dyn || e->pt64) && e->prec != PCSF_PREC_FP64;   // FP64 formation, then FP32 storage
     if (stage64) CK(e->Pbuf64.reserve(max_chunk_ps * (size_t)e->nbr * K2), "cudaMalloc P(t) staging buffer");
     const int nbop = e->nbr - e->nl;
@@ -755,7 +760,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
             CK(launch_pform(true, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, dmv, e->Pbuf64.p, e->dstatus.p + p0, s),
                "P(t) formation launch");
             CK(launch_d2f_rows(e->Pbuf64.p, reinterpret_cast<float *>(e->Pbuf.p), (size_t)(p1 - p0) * e->nbr, e->nbr,
-                               bop, e->nl, s), "P(t) conversion launch");
+                               bop, e->nl, s, dlo), "P(t) conversion launch");
             e->stats.kernel_launches += 1;
         } else if (want_bop && !dyn) {
             CK(launch_pform_tc(e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, e->nl, dmv, e->dPfB.p,
@@ -763,7 +768,8 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
                "tensor-core P(t) formation launch");
         } else {
             CK(launch_pform(e->prec == PCSF_PREC_FP64 || dyn, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, dmv,
-                            e->Pbuf.p, e->dstatus.p + p0, s, false, bop, e->nl), "P(t) formation launch");
+                            e->Pbuf.p, e->dstatus.p + p0, s, false, bop, e->nl, dyn ? nullptr : dlo),
+               "P(t) formation launch");
         }
         CK(cudaEventRecord(e->ev[1], s), "event");
         PruneArgs pa{};
@@ -782,6 +788,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         pa.Bop = bop;
         pa.nbop = nbop;
         pa.dither = e->prec != PCSF_PREC_FP64;
+        pa.dlo = dlo;
         if (grad) {
             GradArgs ga{};
             ga.wi = pa.wi;

@@ -161,7 +161,7 @@ constexpr int PF_BRANCHES = 4;   // branches per CTA (the eigenvectors are stage
 template <typename T>
 __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const double *branch, int nbr,
                                                        DevModels m, T *Pbuf, int32_t *status_key, int raw,
-                                                       float *Bop, int bop_nl)
+                                                       float *Bop, int bop_nl, float *dlo)
 {
     extern __shared__ __align__(16) unsigned char psm[];
     T *UT = reinterpret_cast<T *>(psm);     // [K][K]   UT[m][j] = U[j][m]
@@ -282,33 +282,32 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
             // the diagonal is the compensated sum of the stored (rounded)
             // off-diagonal entries, so every stored row of P = I + E sums to 1
             // to within one rounding of the diagonal; a plain FP32 sum here
-            // biases lpr by ~1e-4 nats per 3000 codons at rho = 1
+            // biases lpr by ~1e-4 nats per 3000 codons at rho = 1.  Branch-free in
+            // j: i differs per lane, and a branch on j == i would split the warp.
             bool neg = false;
             T diag = (T)0, dc = (T)0;
             const T ntol = (T)(-m.tol), dtol = (T)(-1.0 - m.tol);
             for (int j = 0; j < K; j++) {
-                T x = Es[i * (K + 1) + j];
-                if (j == i) {
-                    if (x < dtol) neg = true;      // x + 1 < -tol
-                    continue;
-                }
-                if (x < (T)0) {
-                    if (x < ntol) neg = true;
-                    x = (T)0;
-                    Es[i * (K + 1) + j] = x;
-                }
+                const bool dj = (j == i);
+                const T x0 = Es[i * (K + 1) + j];
+                neg |= dj ? (x0 < dtol) : (x0 < ntol);   // diagonal: x + 1 < -tol
+                const T x = (x0 < (T)0) ? (T)0 : x0;      // an off-diagonal negative within tol becomes 0
+                if (!dj && x != x0) Es[i * (K + 1) + j] = x;
                 if (fp32) {           // Kahan: diag -= x
                     const T y = -x - dc;
                     const T tt = diag + y;
-                    dc = (tt - diag) - y;
-                    diag = tt;
+                    const T c = (tt - diag) - y;
+                    diag = dj ? diag : tt;
+                    dc = dj ? dc : c;
                 } else {
-                    diag -= x;
+                    diag = dj ? diag : diag - x;
                 }
             }
             if (neg) status_min(status_key + r, b, i, PCSF_ENEGP);
             else if (fabs(rs) > m.tol) status_min(status_key + r, b, i, PCSF_EROWSUM);
             else if (!(diag > (T)-1)) status_min(status_key + r, b, i, PCSF_EDIAG);
+            // the sum is diag - dc to second order: its low part for the pruning kernel
+            if (fp32 && dlo) dlo[((size_t)r * nbr + b) * K + i] = (float)(-dc);
             Es[i * (K + 1) + i] = diag;
         }
         __syncthreads();
@@ -329,7 +328,7 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
 }
 
 cudaError_t launch_pform(bool fp64, const PSet *req, int nreq, const double *branch, int nbr, DevModels m,
-                         void *Pbuf, int32_t *status_key, cudaStream_t s, bool raw, float *bop, int bop_nl)
+                         void *Pbuf, int32_t *status_key, cudaStream_t s, bool raw, float *bop, int bop_nl, float *dlo)
 {
     if (nreq <= 0) return cudaSuccess;
     dim3 grid((nbr + PF_BRANCHES - 1) / PF_BRANCHES, nreq);
@@ -338,7 +337,7 @@ cudaError_t launch_pform(bool fp64, const PSet *req, int nreq, const double *bra
         cudaError_t e = cudaFuncSetAttribute(k_pform<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         k_pform<double><<<grid, PF_THREADS, smem, s>>>(req, branch, nbr, m, (double *)Pbuf, status_key, raw ? 1 : 0,
-                                                       nullptr, 0);
+                                                       nullptr, 0, nullptr);
     } else {
         size_t smem = sizeof(float) * (2 * K2 + K * (K + 1) + 2 * K);
         smem = (smem + 15) & ~size_t(15);
@@ -346,7 +345,7 @@ cudaError_t launch_pform(bool fp64, const PSet *req, int nreq, const double *bra
         cudaError_t e = cudaFuncSetAttribute(k_pform<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         k_pform<float><<<grid, PF_THREADS, smem, s>>>(req, branch, nbr, m, (float *)Pbuf, status_key, raw ? 1 : 0,
-                                                      bop, bop_nl);
+                                                      bop, bop_nl, raw ? nullptr : dlo);
     }
     return cudaGetLastError();
 }
@@ -369,7 +368,7 @@ cudaError_t launch_d2f(const double *in, float *out, size_t n, cudaStream_t s)
 // Matrices are [set][nbr]; with bop, the branches b >= bop_nl also get their
 // tensor-core B operand (see bop_store).
 __global__ void __launch_bounds__(256) k_d2f_rows(const double *in, float *out, size_t nmat, int nbr, float *bop,
-                                                  int bop_nl)
+                                                  int bop_nl, float *dlo)
 {
     const size_t mat = blockIdx.x * (size_t)4 + threadIdx.x / K;
     const int i = threadIdx.x % K;
@@ -384,6 +383,7 @@ __global__ void __launch_bounds__(256) k_d2f_rows(const double *in, float *out, 
         d -= (double)x;
     }
     dst[i * K + i] = (float)d;
+    if (dlo) dlo[mat * K + i] = (float)(d - (double)(float)d);   // low part of the diagonal
     const int b = (int)(mat % (size_t)nbr);
     if (bop && b >= bop_nl) {
         float *bd = bop + ((mat / nbr) * (size_t)(nbr - bop_nl) + (b - bop_nl)) * 2 * K2;
@@ -427,10 +427,11 @@ cudaError_t launch_check_codes(const uint8_t *codes, size_t n, unsigned long lon
     return cudaGetLastError();
 }
 
-cudaError_t launch_d2f_rows(const double *in, float *out, size_t nmat, int nbr, float *bop, int bop_nl, cudaStream_t s)
+cudaError_t launch_d2f_rows(const double *in, float *out, size_t nmat, int nbr, float *bop, int bop_nl, cudaStream_t s,
+                            float *dlo)
 {
     if (nmat == 0) return cudaSuccess;
-    k_d2f_rows<<<(unsigned)((nmat + 3) / 4), 256, 0, s>>>(in, out, nmat, nbr, bop, bop_nl);
+    k_d2f_rows<<<(unsigned)((nmat + 3) / 4), 256, 0, s>>>(in, out, nmat, nbr, bop, bop_nl, dlo);
     return cudaGetLastError();
 }
 
@@ -498,6 +499,8 @@ __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
         const Request rq = a.req[wi.request];
         const int md = rq.model;
         const T *Pbase = reinterpret_cast<const T *>(a.Pbuf) + (size_t)rq.pset * a.nbr * K2;
+        // low parts of diag(E) of this P set (FP32 only)
+        const float *dlo = (sizeof(T) == 4 && a.dlo) ? a.dlo + (size_t)rq.pset * a.nbr * K : nullptr;
         const int ncols = wi.ncols;
         const uint8_t *lg = a.leaves + (size_t)wi.col0 * nl;
         // E^T of a node's internal children into shared memory, copied asynchronously one
@@ -541,9 +544,10 @@ __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
             asm volatile("cp.async.wait_all;" ::: "memory");
             __syncthreads();
             T vl[4][CPT], vr[4][CPT];
-            child_partial<T, TC, KAHAN>(Et, slots, sn.lslot, sn.lc, lvT, a0, c0, vl, dcol0, Pbase + (size_t)sn.lc * K2);
+            child_partial<T, TC, KAHAN>(Et, slots, sn.lslot, sn.lc, lvT, a0, c0, vl, dcol0, Pbase + (size_t)sn.lc * K2,
+                                        dlo ? dlo + (size_t)sn.lc * K : nullptr);
             child_partial<T, TC, KAHAN>(Et + K2, slots, sn.rslot, sn.rc, lvT, a0, c0, vr, dcol0,
-                                        Pbase + (size_t)sn.rc * K2);
+                                        Pbase + (size_t)sn.rc * K2, dlo ? dlo + (size_t)sn.rc * K : nullptr);
             __syncthreads();
             if (ni + 1 < a.n_internal) copy_inner(sched[ni + 1]);   // E^T buffers are free again
             MU *cm = colmax + (ni & 1) * TC;

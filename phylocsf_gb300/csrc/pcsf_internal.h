@@ -85,11 +85,14 @@ cudaError_t launch_jacobi(const double *A, double *U, double *lam, int *status, 
 // raw = true skips the row rule (used to form the FP64 grid itself).
 // bop (FP32 only, may be null): tensor-core B operands, [set][nbr - bop_nl][hi, lo][64 x 64],
 // of the branches b >= bop_nl (the branches above internal nodes when bop_nl = n_leaves)
+// dlo (FP32 only, may be null): [set][nbr][K] low parts of the diagonal of E, so that
+// E_ii + dlo_i carries the row rule's diagonal to ~2^-48 (see k_prune)
 cudaError_t launch_pform(bool fp64, const PSet *ps, int nps, const double *branch, int nbr,
                          DevModels m, void *Pbuf, int32_t *status_key, cudaStream_t s, bool raw = false,
-                         float *bop = nullptr, int bop_nl = 0);
+                         float *bop = nullptr, int bop_nl = 0, float *dlo = nullptr);
 cudaError_t launch_d2f(const double *in, float *out, size_t n, cudaStream_t s);
-cudaError_t launch_d2f_rows(const double *in, float *out, size_t nmat, int nbr, float *bop, int bop_nl, cudaStream_t s);
+cudaError_t launch_d2f_rows(const double *in, float *out, size_t nmat, int nbr, float *bop, int bop_nl, cudaStream_t s,
+                            float *dlo = nullptr);
 // Leaf codes of an uploaded batch: *first_bad = the smallest index of a byte > 64
 // (PCSF_MARGINALIZE), left unchanged when every code is valid.
 cudaError_t launch_check_codes(const uint8_t *codes, size_t n, unsigned long long *first_bad, cudaStream_t s);
@@ -111,6 +114,7 @@ struct PruneArgs {
     const void *Bop;         // tensor-core kernel: per chunk-local P set, [nbop][hi, lo][64 x 64] B operands
     int nbop;                //   of the branches above internal nodes (node nl + k)
     int dither;              // SIMT FP32 kernel: per-column dithering of the leaf partials (prune_common.cuh)
+    const float *dlo;        // SIMT FP32 kernel, may be null: per chunk-local P set [nbr][K] low parts of diag(E)
 };
 // comp: 0 plain FP32 sums, 1 Kahan, 2 blocked Kahan (see prune_common.cuh)
 cudaError_t launch_prune(int prec, int comp, const PruneArgs &a, cudaStream_t s, int grid);

@@ -229,9 +229,14 @@ __device__ inline void contract(const T *M, const T *X, int a0, int c0, T out[4]
 // leaf in state s (1 for a marginalised leaf: P rows sum to 1).
 template <typename T, int TC, int KAHAN>
 __device__ inline void child_partial(const T *Et, const T *slots, int slot, int leaf, const uint8_t *lvT, int a0,
-                                     int c0, T v[4][TC / 16], int64_t dither_col0 = -1, const T *leaf_g = nullptr)
+                                     int c0, T v[4][TC / 16], int64_t dither_col0 = -1, const T *leaf_g = nullptr,
+                                     const float *dlo = nullptr)
 {
     constexpr int CPT = TC / 16;
+    // dlo (may be null): the low parts of this branch's diag(E), added to the diagonal
+    // term: FP32 storage of E_ii is the one rounding that every column sharing a state
+    // at this node repeats identically, so over a long region it adds up coherently
+    // (2-3e-3 dB over 10,000 codons at rho = 3 without it)
     if (slot < 0) {
         if (leaf_g) {   // the leaf's E^T rows straight from global memory (4 states per column)
 #pragma unroll
@@ -241,10 +246,12 @@ __device__ inline void child_partial(const T *Et, const T *slots, int slot, int 
                                                : (T)1;
                 T e[4];
                 Vec4<T>::load(leaf_g + (size_t)(s < K ? s : 0) * K + a0, e);
+                // c (1 + E_ss + lo_s) on the diagonal, in one final rounding
+                const T cd = dlo ? fma((T)dlo[s < K ? s : 0], c, c) : c;
 #pragma unroll
                 for (int i = 0; i < 4; i++) {
                     const int a = a0 + i;
-                    v[i][cc] = (s >= K) ? c : fma(e[i], c, (a == s ? c : (T)0));
+                    v[i][cc] = (s >= K) ? c : fma(e[i], c, (a == s ? cd : (T)0));
                 }
             }
             return;
@@ -265,12 +272,17 @@ __device__ inline void child_partial(const T *Et, const T *slots, int slot, int 
     }
     const T *al = slots + (size_t)slot * K * TC;
     contract<T, TC, KAHAN>(Et, al, a0, c0, v);
+    T lo[4] = {(T)0, (T)0, (T)0, (T)0};
+    if (dlo) {
+        const float4 l4 = *reinterpret_cast<const float4 *>(dlo + a0);
+        lo[0] = (T)l4.x; lo[1] = (T)l4.y; lo[2] = (T)l4.z; lo[3] = (T)l4.w;
+    }
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         T x[CPT];
         ColLoad<T, CPT>::load(al + (a0 + i) * TC + c0, x);
 #pragma unroll
-        for (int cc = 0; cc < CPT; cc++) v[i][cc] = x[cc] + v[i][cc];
+        for (int cc = 0; cc < CPT; cc++) v[i][cc] = x[cc] + (dlo ? fma(lo[i], x[cc], v[i][cc]) : v[i][cc]);
     }
 }
 
