@@ -246,12 +246,18 @@ __device__ inline void child_partial(const T *Et, const T *slots, int slot, int 
                                                : (T)1;
                 T e[4];
                 Vec4<T>::load(leaf_g + (size_t)(s < K ? s : 0) * K + a0, e);
-                // c (1 + E_ss + lo_s) on the diagonal, in one final rounding
-                const T cd = dlo ? fma((T)dlo[s < K ? s : 0], c, c) : c;
+                const T lo_s = dlo ? (T)dlo[s < K ? s : 0] : (T)0;
 #pragma unroll
                 for (int i = 0; i < 4; i++) {
                     const int a = a0 + i;
-                    v[i][cc] = (s >= K) ? c : fma(e[i], c, (a == s ? cd : (T)0));
+                    T val = fma(e[i], c, (a == s ? c : (T)0));
+                    if (a == s) {       // + c lo_s: the rounding error r of c (1 + E_ss) is recovered (exactly
+                                        // when P_ss >= 1/2, where c - val is exact), so that lo_s enters
+                                        // the one final rounding instead of vanishing below half an ulp of c
+                        const T r = fma(e[i], c, c - val);
+                        val = val + fma(lo_s, c, r);
+                    }
+                    v[i][cc] = (s >= K) ? c : val;
                 }
             }
             return;
