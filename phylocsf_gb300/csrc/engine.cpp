@@ -588,12 +588,15 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
         return e->fail(PCSF_EINVAL, "tree needs %zu B shared memory for the gradient", gsmem);
     int gper = std::max(1, std::min(4, (int)(prop.sharedMemPerMultiprocessor / (gsmem + 1024))));
     e->grad_grid = prop.multiProcessorCount * gper;
-    // P(t) buffer: up to 4 GiB, at most a quarter of free memory
+    // P(t) buffer: up to 16 GiB, at most a quarter of free memory.  A round of the
+    // search forms one P set per active fit (20,000 fits x 3.6 MB for 58 leaves), so
+    // the chunk size sets how many launch pairs (P(t), pruning) a round takes and how
+    // often a pruning launch ends in a partly filled wave.
     size_t freeb = 0, totalb = 0;
     CK(cudaMemGetInfo(&freeb, &totalb), "cudaMemGetInfo");
     size_t pset_bytes = (size_t)e->nbr * K2 * (e->prec == PCSF_PREC_FP64 ? 8 : 4);
     if (tc) pset_bytes += (size_t)(e->nbr - e->nl) * 2 * K2 * sizeof(float);   // B operands
-    size_t budget = std::min<size_t>(size_t(4) << 30, freeb / 4);
+    size_t budget = std::min<size_t>(size_t(16) << 30, freeb / 4);
     e->pbuf_psets = std::max<size_t>(1, budget / pset_bytes);
     return PCSF_OK;
 }
