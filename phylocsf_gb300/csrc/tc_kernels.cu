@@ -306,6 +306,20 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
             wlf[tid] = (float)a.m.wlog[md * K + tid];
         }
         __syncthreads();
+        // warm L1 with the leaf rows (one 128-byte line per thread and leaf) of the node
+        // after ni, while this node waits for its MMAs or its own gathers
+        auto prefetch_next = [&](int ni) {
+            if (ni + 1 >= a.n_internal) return;
+            const SchedNode nx = sched[ni + 1];
+            if (nx.lslot < 0) {
+                const int sa = lvT[nx.lc * LV_STRIDE + site];
+                asm volatile("prefetch.global.L1 [%0];" :: "l"(Pbase + (size_t)nx.lc * K2 + (size_t)(sa < K ? sa : 0) * K + s0));
+            }
+            if (nx.rslot < 0) {
+                const int sb = lvT[nx.rc * LV_STRIDE + site];
+                asm volatile("prefetch.global.L1 [%0];" :: "l"(Pbase + (size_t)nx.rc * K2 + (size_t)(sb < K ? sb : 0) * K + s0));
+            }
+        };
         int escale = 0;     // this column's sum of rescale exponents
         int kc = 0;         // contractions so far (index into bseq / dreg)
 
@@ -332,6 +346,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
                 if (__syncthreads_or(bad)) { ok = false; break; }
                 tc_fence_after();
                 if (tid == 0) issue_mma(s, r);
+                prefetch_next(ni);      // while the MMAs run
                 if (nint == 1) {
                     const int ls = lvT[lfc * LV_STRIDE + site];
                     leaf_load(Pbase + (size_t)lfc * K2, ls, v);
