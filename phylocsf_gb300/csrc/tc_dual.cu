@@ -158,6 +158,14 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
 
     // one MMA group D(cols) = A B and its completion; false on a timed-out wait
     // (A must be staged and fenced by every thread before the call)
+    // warms L1 with the next node's leaf rows; set per node (none at the last node)
+    const float *pf_a = nullptr, *pf_b = nullptr;
+    auto pf_next_impl = [&]() {
+        if (pf_a) asm volatile("prefetch.global.L1 [%0];" :: "l"(pf_a));
+        if (pf_b) asm volatile("prefetch.global.L1 [%0];" :: "l"(pf_b));
+    };
+    bool pf_on = false;
+    auto pf_next = [&]() { if (pf_on) pf_next_impl(); };
     auto run_mma = [&](uint32_t cols, uint32_t sB, bool need_e) -> bool {
         bool okb = true;
         if (tid == 0 && need_e) {
@@ -172,6 +180,7 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                          :: "r"(barM) : "memory");
         }
+        pf_next();                       // while the MMAs run
         const bool done = mbar_wait(barM, ph_mma);
         ph_mma ^= 1u;
         tc_fence_after();
@@ -236,6 +245,19 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
             // v1 / u1: value and tangent of the first child, then of the node; vt: second child's value.
             // Internal children first; the node's tangent is folded in as the second child's parts
             // arrive (u_p = u_1 v_2 + v_1 u_2), which keeps three 16-value arrays live.
+            pf_on = ni + 1 < a.n_internal;
+            pf_a = pf_b = nullptr;
+            if (pf_on) {
+                const SchedNode nx = sched[ni + 1];
+                if (nx.lslot < 0) {
+                    const int st = lvT[nx.lc * TD_LVS + site];
+                    pf_a = Pbase + (size_t)nx.lc * K2 + (size_t)(st < K ? st : 0) * K + s0;
+                }
+                if (nx.rslot < 0) {
+                    const int st = lvT[nx.rc * TD_LVS + site];
+                    pf_b = Pbase + (size_t)nx.rc * K2 + (size_t)(st < K ? st : 0) * K + s0;
+                }
+            }
             float v1[TD_NS], u1[TD_NS], vt[TD_NS];
             const bool int0 = sn.lslot >= 0 || sn.rslot >= 0;        // is the first child internal?
             const int cA = (sn.lslot >= 0 || sn.rslot < 0) ? sn.lc : sn.rc;
