@@ -565,13 +565,21 @@ __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
             }
             __syncthreads();
             T *out = slots + (size_t)sn.oslot * K * TC;
+            int ecol[CPT];
 #pragma unroll
             for (int cc = 0; cc < CPT; cc++) {
-                T mx = AtomMax<T>::get(cm + c0 + cc);
-                int e = (mx > (T)0) ? exp_of(mx) : 0;
+                const T mx = AtomMax<T>::get(cm + c0 + cc);
+                ecol[cc] = (mx > (T)0) ? exp_of(mx) : 0;
+                if (ty == 0) cscale[c0 + cc] += ecol[cc];
+            }
+            // one vector store per state row (CPT consecutive columns): scalar stores
+            // here were 4-way bank-conflicted
 #pragma unroll
-                for (int i = 0; i < 4; i++) out[(a0 + i) * TC + c0 + cc] = scale2(vl[i][cc], -e);
-                if (ty == 0) cscale[c0 + cc] += e;
+            for (int i = 0; i < 4; i++) {
+                T y[CPT];
+#pragma unroll
+                for (int cc = 0; cc < CPT; cc++) y[cc] = scale2(vl[i][cc], -ecol[cc]);
+                ColStore<T, CPT>::store(out + (a0 + i) * TC + c0, y);
             }
         }
         __syncthreads();

@@ -57,6 +57,24 @@ template <> struct ColLoad<double, 4> {
     static __device__ inline void load(const double *p, double v[4]) { Vec4<double>::load(p, v); }
 };
 
+template <typename T, int CPT> struct ColStore;
+template <> struct ColStore<float, 4> {
+    static __device__ inline void store(float *p, const float v[4]) { *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]); }
+};
+template <> struct ColStore<float, 2> {
+    static __device__ inline void store(float *p, const float v[2]) { *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]); }
+};
+template <> struct ColStore<double, 2> {
+    static __device__ inline void store(double *p, const double v[2]) { *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]); }
+};
+template <> struct ColStore<double, 4> {
+    static __device__ inline void store(double *p, const double v[4])
+    {
+        *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+        *reinterpret_cast<double2 *>(p + 2) = make_double2(v[2], v[3]);
+    }
+};
+
 // P(t) status keys: first error in (branch, row) order wins
 __device__ __forceinline__ void status_min(int32_t *key, int branch, int row, int code)
 {
