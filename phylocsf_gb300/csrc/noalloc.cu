@@ -92,12 +92,14 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
     // reduced-precision engines), as pcsf_lpr does
     const int TC = prec == PCSF_PREC_FP64 ? 32 : 64;
     const size_t es = prec == PCSF_PREC_FP64 ? 8 : 4;
-    // scratch map: [status key][requests][P set][work items][wi_begin][partials]
+    // scratch map: [status key][requests][P set][diag(E) low parts][work items][wi_begin][partials]
     const size_t off_req = 256;
     const size_t off_ps = off_req + ((sizeof(Request) * n_regions + sizeof(PSet) + 255) & ~size_t(255));
     const size_t off_P = off_ps + 256;
     const size_t pbytes = (size_t)nbr * K2 * es;
-    const size_t off_wi = off_P + ((pbytes + 255) & ~size_t(255));
+    const size_t off_dlo = off_P + ((pbytes + 255) & ~size_t(255));
+    const bool fp32 = prec != PCSF_PREC_FP64;
+    const size_t off_wi = off_dlo + (fp32 ? (((size_t)nbr * K * sizeof(float) + 255) & ~size_t(255)) : 0);
     int nwi = 0;
     for (int r = 0; r < n_regions; r++) {
         const int64_t c0 = col_offsets[r], c1 = col_offsets[r + 1];
@@ -124,6 +126,7 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
     Request *d_req = reinterpret_cast<Request *>(sc + off_req);
     PSet *d_ps = reinterpret_cast<PSet *>(sc + off_ps);
     void *d_P = sc + off_P;
+    float *d_dlo = fp32 ? reinterpret_cast<float *>(sc + off_dlo) : nullptr;   // as the allocating path
     WorkItem *d_wi = reinterpret_cast<WorkItem *>(sc + off_wi);
     int32_t *d_wib = reinterpret_cast<int32_t *>(sc + off_wib);
     double *d_part = reinterpret_cast<double *>(sc + off_part);
@@ -135,7 +138,8 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_ps, h_ps, sizeof(PSet), cudaMemcpyHostToDevice, s);
     if (ce == cudaSuccess && nwi) ce = cudaMemcpyAsync(d_wi, h_wi, sizeof(WorkItem) * nwi, cudaMemcpyHostToDevice, s);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_wib, h_wib, sizeof(int32_t) * (n_regions + 1), cudaMemcpyHostToDevice, s);
-    if (ce == cudaSuccess) ce = launch_pform(prec == PCSF_PREC_FP64, d_ps, 1, branch, nbr, m, d_P, d_status, s);
+    if (ce == cudaSuccess)
+        ce = launch_pform(prec == PCSF_PREC_FP64, d_ps, 1, branch, nbr, m, d_P, d_status, s, false, nullptr, 0, d_dlo);
     if (ce == cudaSuccess && nwi) {
         PruneArgs pa{};
         pa.wi = d_wi;
@@ -151,6 +155,7 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
         pa.m = m;
         pa.partials = d_part;
         pa.dither = prec != PCSF_PREC_FP64;     // as pcsf_lpr, so both give the same values
+        pa.dlo = d_dlo;
         const bool tcprec = prec == PCSF_PREC_TF32X3 || prec == PCSF_PREC_TF32;
         ce = launch_prune(prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32, (comp == 0 && tcprec) ? 1 : comp, pa,
                           s, std::min(pgrid, nwi));
