@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
     T *isqT = sqT + K;                        // [K]
     double *ex = reinterpret_cast<double *>(isqT + K);   // [K] expm1(lam t): row-sum identity
     double *cf = ex + K;                                 // [K] GEMM coefficients
-    __shared__ int mode_s, grid_s;
+    __shared__ int mode_s[PF_BRANCHES], grid_s[PF_BRANCHES];
     const int tid = threadIdx.x;
     const int r = blockIdx.y;
     const PSet rq = ps[r];
@@ -192,31 +192,33 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
         isqT[tid] = (T)isq[tid];
     }
     const int ty = tid / 16, tx = tid % 16;
+    // per branch of this CTA, in parallel (one thread each; FP64 is a narrow pipe here):
+    // 0: direct eigen formula (FP64);  1: t == 0;  2: Taylor below the grid;  3: grid correction
+    if (tid < PF_BRANCHES) {
+        const int b = blockIdx.x * PF_BRANCHES + tid;
+        int mode = 0, g = 0;
+        if (b < nbr && fp32 && m.grid_n > 0) {
+            const double t = rq.rho * branch[b];
+            if (t == 0.0) mode = 1;
+            else if (t < m.grid_t[0]) mode = 2;
+            else {
+                mode = 3;
+                double x = log(t / m.grid_t[0]) / m.grid_lr;
+                g = (int)floor(x);
+                if (g < 0) g = 0;
+                if (g > m.grid_n - 1) g = m.grid_n - 1;
+                if (g + 1 < m.grid_n && (m.grid_t[g + 1] - t) < (t - m.grid_t[g])) g++;
+            }
+        }
+        mode_s[tid] = mode;
+        grid_s[tid] = g;
+    }
     for (int bi = 0; bi < PF_BRANCHES; bi++) {
         const int b = blockIdx.x * PF_BRANCHES + bi;
         if (b >= nbr) break;                       // uniform across the block
         const double t = rq.rho * branch[b];
-        __syncthreads();                           // UT ready / previous branch done with smem
-        if (tid == 0) {
-            // 0: direct eigen formula (FP64);  1: t == 0;  2: Taylor below the grid;  3: grid correction
-            int mode = 0, g = 0;
-            if (fp32 && m.grid_n > 0) {
-                if (t == 0.0) mode = 1;
-                else if (t < m.grid_t[0]) mode = 2;
-                else {
-                    mode = 3;
-                    double x = log(t / m.grid_t[0]) / m.grid_lr;
-                    g = (int)floor(x);
-                    if (g < 0) g = 0;
-                    if (g > m.grid_n - 1) g = m.grid_n - 1;
-                    if (g + 1 < m.grid_n && (m.grid_t[g + 1] - t) < (t - m.grid_t[g])) g++;
-                }
-            }
-            mode_s = mode;
-            grid_s = g;
-        }
-        __syncthreads();
-        const int mode = mode_s;
+        __syncthreads();                           // UT and the branch table ready / previous branch done with smem
+        const int mode = mode_s[bi];
         if (tid < K) {
             // ex feeds the row-sum check, which needs it only where w_m != 0
             // (the stationary direction); the FP32 modes therefore spend one
@@ -229,8 +231,8 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
                 if (mode == 3) {
                     // e^{lam t_g} (tabulated) * expm1(lam (t - t_g)) in FP32: the
                     // coefficient is rounded to FP32 for the GEMM in any case
-                    const double h = t - m.grid_t[grid_s];
-                    const float eg = m.grid_eg[((size_t)md * m.grid_n + grid_s) * K + tid];
+                    const double h = t - m.grid_t[grid_s[bi]];
+                    const float eg = m.grid_eg[((size_t)md * m.grid_n + grid_s[bi]) * K + tid];
                     cf[tid] = (double)(eg * expm1f((float)(lam[tid] * h)));
                 }
             }
@@ -256,7 +258,7 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
 #pragma unroll
                     for (int j = 0; j < 4; j++) acc[i][j] += a[i] * bb[j];
             }
-            const float *base = (mode == 3) ? m.gridT + ((size_t)md * m.grid_n + grid_s) * K2 : nullptr;
+            const float *base = (mode == 3) ? m.gridT + ((size_t)md * m.grid_n + grid_s[bi]) * K2 : nullptr;
 #pragma unroll
             for (int i = 0; i < 4; i++)
 #pragma unroll
