@@ -171,6 +171,7 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
     T *isqT = sqT + K;                        // [K]
     double *ex = reinterpret_cast<double *>(isqT + K);   // [K] expm1(lam t): row-sum identity
     double *cf = ex + K;                                 // [K] GEMM coefficients
+    __shared__ T cfT[K];                                 // the same in the storage type
     __shared__ int mode_s[PF_BRANCHES], grid_s[PF_BRANCHES];
     const int tid = threadIdx.x;
     const int r = blockIdx.y;
@@ -226,6 +227,7 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
             if (mode == 0) {
                 ex[tid] = expm1(lam[tid] * t);
                 cf[tid] = ex[tid];
+                cfT[tid] = (T)cf[tid];
             } else {
                 ex[tid] = (wrow[tid] != 0.0) ? (double)expm1f((float)(lam[tid] * t)) : 0.0;   // row-sum check only
                 if (mode == 3) {
@@ -234,6 +236,7 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
                     const double h = t - m.grid_t[grid_s[bi]];
                     const float eg = m.grid_eg[((size_t)md * m.grid_n + grid_s[bi]) * K + tid];
                     cf[tid] = (double)(eg * expm1f((float)(lam[tid] * h)));
+                    cfT[tid] = (T)cf[tid];
                 }
             }
         }
@@ -241,9 +244,20 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
         if (mode == 0 || mode == 3) {
             for (int f = tid; f < K2; f += PF_THREADS) {
                 int mm = f / K;
-                UeT[f] = UT[f] * (T)cf[mm];
+                UeT[f] = UT[f] * cfT[mm];
             }
             __syncthreads();
+            // E(t_g) (stored transposed) for this thread's 4 x 4 block, loaded before the
+            // GEMM: one 16-byte load per column jj (rows 4 ty .. 4 ty + 3)
+            float gb[4][4];
+            if (mode == 3) {
+                const float *base = m.gridT + ((size_t)md * m.grid_n + grid_s[bi]) * K2;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const float4 q = __ldg(reinterpret_cast<const float4 *>(base + (size_t)(4 * tx + j) * K + 4 * ty));
+                    gb[j][0] = q.x; gb[j][1] = q.y; gb[j][2] = q.z; gb[j][3] = q.w;
+                }
+            }
             T acc[4][4];
 #pragma unroll
             for (int i = 0; i < 4; i++)
@@ -258,14 +272,13 @@ __global__ void __launch_bounds__(PF_THREADS) k_pform(const PSet *ps, const doub
 #pragma unroll
                     for (int j = 0; j < 4; j++) acc[i][j] += a[i] * bb[j];
             }
-            const float *base = (mode == 3) ? m.gridT + ((size_t)md * m.grid_n + grid_s[bi]) * K2 : nullptr;
 #pragma unroll
             for (int i = 0; i < 4; i++)
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     int ii = 4 * ty + i, jj = 4 * tx + j;
                     T v = acc[i][j] * sqT[jj] * isqT[ii];
-                    if (base) v += (T)base[jj * K + ii];
+                    if (mode == 3) v += (T)gb[j][i];
                     Es[ii * (K + 1) + jj] = v;
                 }
         } else {
