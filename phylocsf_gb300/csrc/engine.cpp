@@ -25,6 +25,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <unordered_map>
 #include <string>
 #include <utility>
 #include <vector>
@@ -650,7 +651,17 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     std::vector<WorkItem> wis;
     std::vector<PSet> psets;
     std::vector<int> chunk_req_begin, chunk_ps_begin;   // chunk boundaries
-    std::map<std::pair<int, uint64_t>, int> cur;
+    // (model, rho bits) -> chunk-local P set; a hash map: a search round asks for
+    // ~20,000 distinct tree scales, and an ordered map's lookups showed in the host time
+    struct PsKeyHash {
+        size_t operator()(const std::pair<int, uint64_t> &k) const
+        {
+            return std::hash<uint64_t>()(k.second * 0x9E3779B97F4A7C15ull + (uint64_t)(uint32_t)k.first);
+        }
+    };
+    std::unordered_map<std::pair<int, uint64_t>, int, PsKeyHash> cur;
+    cur.reserve(std::min<size_t>((size_t)nreq, e->pbuf_psets) * 2);
+    wis.reserve((size_t)nreq * 8);
     chunk_req_begin.push_back(0);
     chunk_ps_begin.push_back(0);
     std::vector<int> req_pset_global(nreq);
@@ -1173,8 +1184,11 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
         gowner.clear();
         areqs.clear();
         aowner.clear();
+        std::vector<double> need, needg, needa;     // reused across fits (no allocation per fit)
         for (int i = 0; i < (int)fits.size(); i++) {
-            std::vector<double> need, needg, needa;
+            need.clear();
+            needg.clear();
+            needa.clear();
             advance(fits[i], need, needg, needa);
             for (auto *lst : {&need, &needg, &needa}) {
                 std::sort(lst->begin(), lst->end());
