@@ -23,12 +23,15 @@
 //  - shared form (every region is live, e.g. 6 of the 56 contractions of the
 //    58-leaf tree): hi and lo both go to the shared-memory A operand and D is
 //    written over the child's own slot.
-// The shared-memory data pipe is what bounds this kernel: the tensor cores' operand
-// reads share it with the threads' loads and stores.  The region form moves 80 KB
-// of operand reads per contraction instead of 144 KB, and 64 KB of thread traffic
-// instead of 128 KB.  Both forms issue the same MMAs in the same order on the same
-// values, so their results are identical.  The epilogue reads alpha_c = hi + lo
-// back from where the staging put them.
+// The region form moves 80 KB of shared-memory operand reads per contraction
+// instead of 144 KB, and 64 KB of thread traffic instead of 128 KB.  Both forms issue
+// the same MMAs in the same order on the same values, so their results are
+// identical.  The epilogue reads alpha_c = hi + lo back from where the staging put
+// them.  What bounds the kernel is the latency of the per-node chain (MMA issue and
+// completion, the epilogue, the leaf gathers, the barriers), which the two CTAs on an
+// SM overlap: the MMA descriptors are precomputed, the leaf rows are gathered with
+// 256-bit loads, and while a node's MMAs run its threads prefetch into L1 the leaf
+// rows of the next node.
 //
 // Shared memory (about 106 KB for 58 leaves): one A operand (128 x 64, hi + lo),
 // one B operand (64 x 64, hi + lo), the tile's leaf states and the schedule.
@@ -38,7 +41,9 @@
 // (cp.async.bulk, completion on an mbarrier), issued as soon as the previous
 // contraction has released the buffer.  Leaf children are gathers of E^T rows
 // from L2 while the MMAs run.  The per-column rescale exponent is the maximum
-// over the two threads of a column.
+// over the two threads of a column.  The root stage forms z = pi . alpha as an FP32
+// compensated dot product and log z = log m + e ln 2 (m in [0.5, 1)), with FP64
+// only for the per-column log and the tile sums.
 //
 // Accuracy: the tensor cores' FP32 accumulation is not round-to-nearest: it
 // rounds toward minus infinity (a measured mean of -5.7 ulp of the result over
