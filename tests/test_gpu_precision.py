@@ -57,3 +57,28 @@ def test_120mammals_precision(workload, reference, prec, rel_bound, db_bound):
         assert rel.max() <= rel_bound
     if db_bound is not None:
         assert ddb.max() <= db_bound
+
+
+def test_long_regions_fixed_rho():
+    """Returned values of the FP32 engine on long 100vertebrates regions at fixed rho, against
+    FP64: |d score| grows roughly linearly with length (partly coherent FP32 rounding of the
+    partials).  Measured max: 3.0e-4 dB at 2,000 codons, 8.8e-4 dB at 5,000 codons (rho = 1);
+    the bounds are about twice that, to catch a regression of the compensation, the dithering
+    or the diagonal low parts."""
+    ps = synth.load_params("100vertebrates")
+    rng = np.random.default_rng(11)
+    lengths = np.array([2000] * 8 + [5000] * 8)
+    models = (rng.random(len(lengths)) >= 0.25).astype(np.int32)
+    gf = synth.gap_fractions(rng, len(lengths), ps.tree.nl, 0.05, 0.40, 0.0)
+    offs, lv = synth.simulate(ps, lengths, models, gf, 5)
+    out = {}
+    for prec in ("fp64", "fp32b"):
+        e = P.Engine(ps.tree, ps.S_c, ps.pi_c, ps.S_n, ps.pi_n, precision=prec)
+        b = e.batch(offs, lv)
+        out[prec] = (e.lpr(b, 0, 1.0)[0], e.lpr(b, 1, 1.0)[0])
+        e.close()
+    (c0, n0), (c, n) = out["fp64"], out["fp32b"]
+    ddb = np.abs(10.0 * ((c - n) - (c0 - n0)) / np.log(10.0))
+    print("2,000 codons max %.2e dB; 5,000 codons max %.2e dB" % (ddb[:8].max(), ddb[8:].max()))
+    assert ddb[:8].max() <= 6e-4
+    assert ddb[8:].max() <= 1.8e-3
