@@ -332,12 +332,19 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
             const SchedNode sn = sched[ni];
             float v[32];
             // internal children are contracted one after the other (l before r); a
-            // leaf child beside an internal one is gathered while the MMAs run (loading
-            // it before the staging measured slower).  Every barrier also agrees on a
-            // timed-out wait (bad), so that all threads leave together.
+            // leaf child beside an internal one is gathered while the MMAs run, except by
+            // warp 0, whose thread 0 issues them (all warps loading before the staging
+            // measured slower).  Every barrier also agrees on a timed-out wait (bad), so
+            // that all threads leave together.
             const int slotL = sn.lslot, slotR = sn.rslot;
             const int nint = (slotL >= 0) + (slotR >= 0);
             const int lfc = (slotL < 0) ? sn.lc : sn.rc;   // the leaf child when nint == 1
+            // warp 0 (whose thread 0 issues the MMAs) loads its leaf rows before the staging
+            int ls0 = K;
+            if (nint == 1 && warp == 0) {
+                ls0 = lvT[lfc * LV_STRIDE + site];
+                leaf_load(Pbase + (size_t)lfc * K2, ls0, v);
+            }
             bool have = (nint == 1), bad = false;
             int nc = 0;
             for (int side = 0; side < 2; side++) {
@@ -353,9 +360,11 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
                 if (tid == 0) issue_mma(s, r);
                 prefetch_next(ni);      // while the MMAs run
                 if (nint == 1) {
-                    const int ls = lvT[lfc * LV_STRIDE + site];
-                    leaf_load(Pbase + (size_t)lfc * K2, ls, v);
-                    leaf_fix(ls, v);
+                    if (warp != 0) {
+                        ls0 = lvT[lfc * LV_STRIDE + site];
+                        leaf_load(Pbase + (size_t)lfc * K2, ls0, v);
+                    }
+                    leaf_fix(ls0, v);
                 }
                 const bool done = mbar_wait(barM, ph_mma);
                 ph_mma ^= 1u;
