@@ -177,7 +177,9 @@ int pcsf_engine_pt(pcsf_engine *e, int32_t model, int32_t n_t, const double *t, 
 /* Upload a batch of regions.  Region r is columns [col_offsets[r],
  * col_offsets[r+1]); leaves is [total_cols][n_leaves] uint8 codon indices
  * 16*n1+4*n2+n3 (Code.ml:140-141), PCSF_MARGINALIZE for a marginalised leaf
- * (this packs PhyloCSF.pleaves' output, PhyloCSF.ml:219-246). */
+ * (this packs PhyloCSF.pleaves' output, PhyloCSF.ml:219-246).  The codes are
+ * checked on the device after the upload; a code above PCSF_MARGINALIZE fails the
+ * call with PCSF_EINVAL, naming the first bad column and leaf. */
 int pcsf_batch_create(pcsf_engine *e, int32_t n_regions, const int64_t *col_offsets, const uint8_t *leaves,
                       pcsf_batch **out);
 void pcsf_batch_destroy(pcsf_batch *b);
