@@ -639,7 +639,8 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         return e->fail(PCSF_EINVAL, "d lpr / d rho by the tangent pass needs a tensor-core engine and a tree of <= 4 slots");
     const bool tc = (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32) && !accurate;
     // the gradient always runs the SIMT adjoint kernel (64-column tiles in FP32)
-    const int TC = (grad || !tc) ? (e->prec == PCSF_PREC_FP64 ? 32 : 64) : prune_tile_cols(e->prec);
+    const int TC = grad ? (e->prec == PCSF_PREC_FP64 ? 32 : 64)
+                        : !tc ? simt_tile_cols(e->prec, e->nslots) : prune_tile_cols(e->prec);
     const int comp = (accurate && (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32)) ? e->accurate_comp()
                                                                                               : e->comp_mode();
 

@@ -90,7 +90,7 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
     if (col_offsets[0] != 0) return pcsf_internal_fail(e, PCSF_EINVAL, "pcsf_lpr_noalloc: col_offsets[0] must be 0");
     // every returned likelihood comes from the SIMT kernels (compensated FP32 on
     // reduced-precision engines), as pcsf_lpr does
-    const int TC = prec == PCSF_PREC_FP64 ? 32 : 64;
+    const int TC = simt_tile_cols(prec, nslots);
     const size_t es = prec == PCSF_PREC_FP64 ? 8 : 4;
     // scratch map: [status key][requests][P set][diag(E) low parts][work items][wi_begin][partials]
     const size_t off_req = 256;

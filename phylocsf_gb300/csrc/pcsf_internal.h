@@ -119,6 +119,7 @@ struct PruneArgs {
 // comp: 0 plain FP32 sums, 1 Kahan, 2 blocked Kahan (see prune_common.cuh)
 cudaError_t launch_prune(int prec, int comp, const PruneArgs &a, cudaStream_t s, int grid);
 int prune_tile_cols(int prec);
+int simt_tile_cols(int prec, int nslots);   // the SIMT kernel's column tile (k_prune)
 size_t prune_smem_bytes(int prec, int nslots, int nl, int nint);
 
 // Adjoint gradient over work items (grad_kernels.cu): per work item the lpr /
