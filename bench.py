@@ -13,11 +13,17 @@ rho MLE).  Inputs (7.2 M columns x 58 leaves, ~0.42 GB) are larger than L2.
   roofline    the pruning kernel: algorithmic FLOPs (8192(nl-2)+64(nl-1)+128
               per column-evaluation) / its device time
   cpu_baseline  the FP64 oracle port (the reference's loop structure, dense
-              leaves) on a bounded sample of regions, one process per core
+              leaves) on a length-stratified sample of regions, a persistent
+              pool of one process per core fed longest-first
+  fp64_gpu    the plain FP64 GPU path (oracle-matched iterates) timed on a
+              length-stratified sample of the same workload: the denominator of
+              the split-precision engine's speed-up
 
 ``--impl reference`` times that CPU port alone (the reference is OCaml + GSL,
-which cannot be built here).  Multi-GPU (torchrun): replicas, each rank scores
-its own workload (no data-path collective), weak scaling.
+which cannot be built here).  It builds its sample of regions with the numpy
+restatement of the column simulator (oracle/synth_np.py) and never loads the
+engine library.  Multi-GPU (torchrun): replicas, each rank scores its own
+workload (no data-path collective), weak scaling.
 """
 from __future__ import annotations
 
@@ -37,6 +43,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "codon-column·branches/s and regions scored/s at |Δscore|≤1e-3 dB vs FP64 oracle"
+DATA = "synthetic (seeded simulation along the tree; no public benchmark exists)"
 L2_BYTES = 129 * 1024 * 1024
 DTYPES = {"fp32": "f32", "fp32c": "f32 (compensated)", "fp32b": "f32 (blocked compensation)", "fp64": "f64",
           "tf32x3": "tf32x3 search, f32 (compensated) reported",
@@ -140,90 +147,177 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU port
-def _cpu_worker(args):
-    name, lv, strategy = args
+_CPU = {}
+
+
+def _cpu_init(name: str):
+    """Pool initialiser: the oracle's models of parameter set `name`, the reference's dense loop."""
     from oracle import oracle as O
-    from tests import helpers as H
-    O.set_sparse_leaves(False)          # the reference's dense loop
-    mc, mn, ot, tree = H.oracle_models(name)
+    from phylocsf_gb300 import synth
+    ps = synth.load_params(name)
+    t = ps.tree
+    n = t.n
+    lch = np.full(n, -1, np.int32)
+    rch = np.full(n, -1, np.int32)
+    for i in range(n - 1):
+        p = t.parent[i]
+        if lch[p] < 0:
+            lch[p] = i
+        else:
+            rch[p] = i
+    ot = O.OTree(O.Tree(t.labels, t.parent, lch, rch, t.branch))
+    _CPU.update(O=O, mc=O.OModel.from_ecm(ps.S_c, ps.pi_c), mn=O.OModel.from_ecm(ps.S_n, ps.pi_n), ot=ot)
+    O.set_sparse_leaves(False)          # the reference's dense loop (PhyloLik.ml:87-90)
+
+
+def _cpu_noop(_):
+    return os.getpid()
+
+
+def _cpu_worker(job):
+    key, lv, strategy = job
+    O = _CPU["O"]
+    x = lv.astype(np.int32)
+    x[x >= 64] = -1
     t0 = time.perf_counter()
-    r = O.score_region(mc, mn, ot, strategy, H.u8_to_oracle(lv))
-    return r.score, r.status, r.evals, time.perf_counter() - t0
+    r = O.score_region(_CPU["mc"], _CPU["mn"], _CPU["ot"], strategy, x)
+    return key, r.score, r.status, r.evals, time.perf_counter() - t0
 
 
-def cpu_port_sample(name: str, offs, leaves, strategy: int, idx, cores: int):
-    """Score regions idx with the FP64 oracle port, one process per core (spawned)."""
-    jobs = [(name, leaves[offs[i]:offs[i + 1]].copy(), strategy) for i in idx]
-    ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
-    with ctx.Pool(cores) as pool:
-        out = pool.map(_cpu_worker, jobs, chunksize=1)
-    wall = time.perf_counter() - t0
-    return out, wall
+class CpuPool:
+    """A persistent pool of one process per core (spawned, so no CUDA context crosses a fork),
+    started and warmed up outside any timed region.  score() feeds a region list longest-first,
+    one region per task, as the reference's `-p N` mode schedules its region list
+    (src/PhyloCSF.ml:303-308)."""
+
+    def __init__(self, name: str, cores: int):
+        self.cores = cores
+        self.pool = mp.get_context("spawn").Pool(cores, initializer=_cpu_init, initargs=(name,))
+        self.pool.map(_cpu_noop, range(cores), chunksize=1)
+
+    def score(self, jobs):
+        """jobs: (key, leaves uint8 [L][nl], strategy); returns {key: (score, status, evals, seconds)}, wall."""
+        order = sorted(jobs, key=lambda j: -j[1].shape[0])
+        t0 = time.perf_counter()
+        out = {k: v for k, *v in self.pool.imap_unordered(_cpu_worker, order, chunksize=1)}
+        return out, time.perf_counter() - t0
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
 
 
-def pick_sample(offs, n, seed=123):
-    rng = np.random.default_rng(seed)
-    R = len(offs) - 1
-    return np.sort(rng.choice(R, size=min(n, R), replace=False))
+def stratified(col_offsets, n: int, offset: int = 0):
+    """n regions at evenly spaced length quantiles (sorted by length, ties by index)."""
+    L = np.diff(col_offsets)
+    order = np.lexsort((np.arange(len(L)), L))
+    n = min(n, len(L))
+    pos = np.unique(np.linspace(0, len(L) - 1, n).round().astype(np.int64))
+    return order[(pos + offset) % len(L)]
+
+
+def sample_leaves_np(spec, idx):
+    """Leaf codes of regions idx of a workload, from the numpy restatement of the simulator."""
+    from oracle import synth_np
+    from phylocsf_gb300 import synth
+    P, prior = synth.simulation_inputs(spec.params)
+    out, L = [], np.diff(spec.col_offsets)
+    lv = synth_np.simulate_regions(spec.params.tree.parent, P, prior, spec.col_offsets, spec.models, spec.gap_frac,
+                                   spec.seed, idx)
+    o = 0
+    for r in idx:
+        out.append(lv[o:o + L[r]])
+        o += L[r]
+    return out
+
+
+def loaded_native_libs():
+    """Shared libraries from this repository mapped into this process."""
+    libs = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                path = line.split()[-1] if len(line.split()) >= 6 else ""
+                if path.startswith(ROOT) and ".so" in path:
+                    libs.add(os.path.relpath(path, ROOT))
+    except OSError:
+        pass
+    return sorted(libs)
+
+
+def workload_config(spec, world: int) -> dict:
+    """The workload description both arms print (identical keys and values)."""
+    nbytes = spec.total_cols * spec.params.tree.nl
+    return {"workload": spec.name, "tree": spec.params.name, "strategy": "mle" if spec.strategy else "fixed",
+            "regions_per_gpu": spec.n_regions, "columns_per_gpu": spec.total_cols,
+            "l2": ("L2 flushed before every timed step (inputs %.0f MB)" if nbytes < 2 * L2_BYTES
+                   else "inputs larger than L2 (%.0f MB)") % (nbytes / 1e6),
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 # ---------------------------------------------------------------- reference arm
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    from phylocsf_gb300 import synth
-    wl = make_workload(args, seed=0)
+    spec = make_spec(args, seed=0)
     cores = args.cpu_cores or os.cpu_count() or 1
-    nb = wl.params.tree.n - 1
-    times, regions, colb = [], 0, 0
-    step = 0
-    for it in range(args.warmup + args.steps):
-        idx = pick_sample(wl.col_offsets, cores, seed=1000 + it)
-        out, wall = cpu_port_sample(wl.params.name, wl.col_offsets, wl.leaves, wl.strategy, idx, cores)
-        if it >= args.warmup:
-            times.append(wall)
-            regions += len(idx)
-            colb += int(sum(wl.col_offsets[i + 1] - wl.col_offsets[i] for i in idx)) * nb
-            step += 1
-    total = sum(times)
-    v = regions / total
-    line = {"metric": METRIC, "value": v, "unit": "regions/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000 * total / max(step, 1), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": wl.name, "strategy": "mle" if wl.strategy else "fixed", "tree": wl.params.name,
-                       "regions": wl.n_regions},
+    nb = spec.params.tree.n - 1
+    K = args.steps
+    per_step = max(1, -(-args.ref_regions // K))
+    sample = stratified(spec.col_offsets, per_step * K)
+    steps = [sample[k::K] for k in range(K)]                 # each step a stratified slice
+    warm = stratified(spec.col_offsets, 4 * cores)[:cores]   # the shortest regions: warm-up only
+    lv = dict(zip(list(sample) + list(warm), sample_leaves_np(spec, list(sample) + list(warm))))
+    pool = CpuPool(spec.params.name, cores)
+    for _ in range(args.warmup):
+        pool.score([(int(r), lv[r], spec.strategy) for r in warm])
+    # the K steps' regions go to the pool as one longest-first list, so no core idles at a
+    # step boundary; ms_per_step = wall / K
+    jobs = [(int(r), lv[r], spec.strategy) for st in steps for r in st]
+    out, wall = pool.score(jobs)
+    pool.close()
+    regions = len(jobs)
+    L = np.diff(spec.col_offsets)
+    cols = int(sum(L[r] for r in sample))
+    v = regions / wall
+    line = {"metric": METRIC, "value": v, "unit": "regions/s", "n_gpus": world, "steps": K,
+            "warmup": args.warmup, "ms_per_step": 1000 * wall / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA, "impl": "reference",
+            "config": workload_config(spec, world),
             "cpu_baseline": {"value": v, "unit": "regions/s", "cores": cores, "kind": "port",
-                             "sample": "%d random regions per step of the workload, one process per core, "
-                                       "FP64 oracle with the reference's dense loop" % cores},
+                             "sample": "%d regions (%d codon columns) at evenly spaced length quantiles of the "
+                                       "workload, %d per step, fed longest-first to a persistent pool of %d "
+                                       "processes (nproc %d); FP64 oracle with the reference's dense loop"
+                                       % (regions, cols, per_step, cores, os.cpu_count() or 0)},
             "e2e": {"value": v, "unit": "regions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "column_branches_per_s": colb / total,
+            "column_branches_per_s": sum(o[2] * L[k] for k, o in out.items()) * nb / wall,
+            "columns_per_s": cols / wall,
+            "evaluations": int(sum(o[2] for o in out.values())),
+            "failed_regions": int(sum(1 for o in out.values() if o[1] != 0)),
+            "native_libs_loaded": loaded_native_libs(),
             "note": "the reference is OCaml+GSL and cannot be built on this image; this arm times the C FP64 "
-                    "restatement of its loop structure"}
+                    "restatement of its loop structure (oracle/)"}
     print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------- our arm
-def make_workload(args, seed):
-    wl = _make_workload(args, seed)
-    if args.strategy is not None:
-        import phylocsf_gb300 as P
-        wl.strategy = P.FIXED if args.strategy == "fixed" else P.MLE
-        wl.name = wl.name.replace("_mle", "_" + args.strategy).replace("_fixed", "_" + args.strategy)
-    return wl
-
-
-def _make_workload(args, seed):
+def make_spec(args, seed):
     from phylocsf_gb300 import synth
+    import phylocsf_gb300 as P
     if args.workload == "58mammals_mle":
-        return synth.workload_58mammals_mle(n_regions=args.regions, seed=seed)
-    if args.workload == "12flies_fixed":
-        return synth.workload_12flies_fixed(seed=seed)
-    if args.workload == "120mammals_fixed":
-        return synth.workload_120mammals_fixed(total_cols=args.cols, seed=seed)
-    if args.workload == "100vertebrates_mle":
-        return synth.workload_100vertebrates_mle(n_regions=args.regions, seed=seed)
-    raise SystemExit("unknown workload " + args.workload)
+        spec = synth.spec_58mammals_mle(n_regions=args.regions, seed=seed)
+    elif args.workload == "12flies_fixed":
+        spec = synth.spec_12flies_fixed(seed=seed)
+    elif args.workload == "120mammals_fixed":
+        spec = synth.spec_120mammals_fixed(total_cols=args.cols, seed=seed)
+    elif args.workload == "100vertebrates_mle":
+        spec = synth.spec_100vertebrates_mle(n_regions=args.regions, seed=seed)
+    else:
+        raise SystemExit("unknown workload " + args.workload)
+    if args.strategy is not None:
+        spec.strategy = P.FIXED if args.strategy == "fixed" else P.MLE
+        spec.name = spec.name.replace("_mle", "_" + args.strategy).replace("_fixed", "_" + args.strategy)
+    return spec
 
 
 def load_peaks():
@@ -248,7 +342,9 @@ def run_ours(args, world, rank, local):
     import torch
     import phylocsf_gb300 as P
 
-    wl = make_workload(args, seed=rank)
+    from phylocsf_gb300 import synth
+    spec = make_spec(args, seed=rank)
+    wl = synth.realize(spec)
     ps = wl.params
     nl = ps.tree.nl
     nb = ps.tree.n - 1
@@ -338,13 +434,10 @@ def run_ours(args, world, rank, local):
     line = {"metric": METRIC, "value": value, "unit": "regions/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": DTYPES.get(args.precision, args.precision),
-            "data": "synthetic (seeded simulation along the tree; no public benchmark exists)",
-            "config": {"workload": wl.name, "tree": ps.name, "strategy": "mle" if wl.strategy else "fixed",
-                       "regions_per_gpu": wl.n_regions, "columns_per_gpu": wl.total_cols,
-                       "precision": args.precision, "l2": ("L2 flushed before every timed step (inputs %.0f MB)" if flush is not None
-                              else "inputs larger than L2 (%.0f MB)") % (wl.leaves.nbytes / 1e6),
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "ctas": {"simt_prune": st["prune_grid"], "tensor_core_prune": st["tc_grid"]}},
+            "data": DATA,
+            "config": workload_config(spec, world),
+            "precision": args.precision,
+            "launch": {"ctas": {"simt_prune": st["prune_grid"], "tensor_core_prune": st["tc_grid"]}},
             "column_branches_per_s": colb_per_s,
             "e2e": {"value": e2e_value, "unit": "regions/s", "h2d_bytes_per_step": int(wl.leaves.nbytes +
                                                                                        wl.col_offsets.nbytes),
@@ -388,33 +481,74 @@ def run_ours(args, world, rank, local):
                            "region_latency_ms_p99": float(np.percentile(done_ms, 99)),
                            "throughput_regions_per_s": wl.n_regions / total_s,
                            "clock": "host wall clock around each call (synchronous API)"}
-    if rank == 0 and not args.no_accuracy:
-        acc = {}
-        # (a) against the FP64 GPU path on a subsample
-        sub = pick_sample(wl.col_offsets, args.fp64_regions, seed=7)
+    if rank == 0 and not args.no_fp64:
+        # the plain FP64 GPU path (oracle-matched iterates) on a length-stratified sample: the
+        # the benchmark spec's denominator (time) and the accuracy reference (scores)
+        sub = stratified(wl.col_offsets, args.fp64_regions)
         parts = [wl.leaves[wl.col_offsets[i]:wl.col_offsets[i + 1]] for i in sub]
         so = np.zeros(len(sub) + 1, np.int64)
         so[1:] = np.cumsum([p.shape[0] for p in parts])
         e64 = P.Engine(ps.tree, ps.S_c, ps.pi_c, ps.S_n, ps.pi_n, precision="fp64", device=local)
-        r64 = e64.score_batch(so, np.concatenate(parts), wl.strategy)
+        s64 = torch.cuda.ExternalStream(e64.stream_handle(), device=torch.device("cuda", local))
+        b64 = e64.batch(so, np.concatenate(parts))
+        warm = e64.batch(so[:9] - so[0], np.concatenate(parts[:8]))   # first launches (attributes, module load)
+        e64.score(warm, wl.strategy)
+        warm.close()
+        torch.cuda.synchronize(local)
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(s64)
+        r64 = e64.score(b64, wl.strategy)
+        f1.record(s64)
+        f1.synchronize()
+        ms64 = f0.elapsed_time(f1)
+        # the split-precision engine on the same sample, same clock, for a like-for-like ratio
+        bs = eng.batch(so, np.concatenate(parts))
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(local)
+        g0.record(stream)
+        rs = eng.score(bs, wl.strategy)
+        g1.record(stream)
+        g1.synchronize()
+        ms_s = g0.elapsed_time(g1)
+        bs.close()
+        b64.close()
         e64.close()
         d = np.abs(r64["score"] - res["score"][sub])
-        acc["vs_fp64_gpu"] = {"regions": int(len(sub)), "max_abs_db": float(d.max()),
-                              "median_abs_db": float(np.median(d)), "frac_le_1e-3_db": float((d <= 1e-3).mean())}
-        line["accuracy"] = acc
+        line["fp64_gpu"] = {"regions": int(len(sub)), "columns": int(so[-1]), "ms": ms64,
+                            "value": len(sub) / (ms64 / 1000.0), "unit": "regions/s",
+                            "split_precision_ms_same_sample": ms_s,
+                            "speedup_same_sample": ms64 / ms_s,
+                            "speedup_vs_headline_value": value / (len(sub) / (ms64 / 1000.0)),
+                            "sample": "regions at evenly spaced length quantiles of the workload"}
+        line.setdefault("accuracy", {})["vs_fp64_gpu"] = {
+            "regions": int(len(sub)), "max_abs_db": float(d.max()), "median_abs_db": float(np.median(d)),
+            "frac_le_1e-3_db": float((d <= 1e-3).mean()),
+            "failed": int((r64["status"] != 0).sum() + (res["status"][sub] != 0).sum()),
+            "same_scores_on_sample": bool(np.array_equal(rs["score"], res["score"][sub]))}
     if rank == 0 and not args.no_cpu_baseline:
+        # the FP64 oracle port (the reference's dense loop) on a length-stratified sample: its time
+        # is the CPU baseline, its scores the oracle check of the returned scores
         cores = args.cpu_cores or os.cpu_count() or 1
-        idx = pick_sample(wl.col_offsets, cores, seed=99)
-        out, wall = cpu_port_sample(ps.name, wl.col_offsets, wl.leaves, wl.strategy, idx, cores)
-        d = np.abs(np.array([o[0] for o in out]) - res["score"][idx])
+        idx = stratified(wl.col_offsets, args.cpu_regions, offset=1)
+        pool = CpuPool(ps.name, cores)
+        out, wall = pool.score([(int(i), wl.leaves[wl.col_offsets[i]:wl.col_offsets[i + 1]], wl.strategy)
+                                for i in idx])
+        pool.close()
+        d = np.abs(np.array([out[int(i)][0] for i in idx]) - res["score"][idx])
         cols = int(sum(wl.col_offsets[i + 1] - wl.col_offsets[i] for i in idx))
         line["cpu_baseline"] = {"value": len(idx) / wall, "unit": "regions/s", "cores": cores, "kind": "port",
-                                "sample": "%d random regions (%d codon columns) of the workload, one process per "
-                                          "core, FP64 oracle with the reference's dense loop" % (len(idx), cols),
+                                "sample": "%d regions (%d codon columns) at evenly spaced length quantiles of the "
+                                          "workload, fed longest-first to a persistent pool of %d processes "
+                                          "(nproc %d); FP64 oracle with the reference's dense loop"
+                                          % (len(idx), cols, cores, os.cpu_count() or 0),
                                 "wall_s": wall}
         line.setdefault("accuracy", {})["vs_fp64_oracle"] = {
-            "regions": int(len(idx)), "max_abs_db": float(d.max()), "frac_le_1e-3_db": float((d <= 1e-3).mean())}
+            "regions": int(len(idx)), "max_abs_db": float(d.max()), "median_abs_db": float(np.median(d)),
+            "frac_le_1e-3_db": float((d <= 1e-3).mean())}
     if rank == 0:
+        line["native_libs_loaded"] = loaded_native_libs()
         print(json.dumps(line), flush=True)
     batch.close()
     eng.close()
@@ -432,9 +566,14 @@ def main():
     ap.add_argument("--precision", default="tf32x3b")
     ap.add_argument("--strategy", default=None, choices=[None, "fixed", "mle"],
                     help="override the workload's strategy (fixed: one likelihood pass, used for profiling)")
-    ap.add_argument("--fp64-regions", type=int, default=256)
+    ap.add_argument("--fp64-regions", type=int, default=1024,
+                    help="regions of the workload timed on the FP64 GPU path (and compared with it)")
+    ap.add_argument("--cpu-regions", type=int, default=64,
+                    help="regions of the workload timed on the CPU port (and compared with it)")
+    ap.add_argument("--ref-regions", type=int, default=128,
+                    help="reference arm: regions timed over all steps")
     ap.add_argument("--cpu-cores", type=int, default=0)
-    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--latency-batches", type=int, default=0,
                     help="also score the workload as this many consecutive batches and report latency percentiles")

@@ -224,11 +224,15 @@ int pcsf_grad(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, d
  * that cannot take cudaMalloc's implicit synchronisation, a process at a hard
  * device-memory cap).  d_leaves ([total_cols][n_leaves], codes as in
  * pcsf_batch_create), d_lpr and d_elpr ([n_regions]; d_elpr may be NULL) are
- * DEVICE pointers owned by the caller; col_offsets is a host array.  Scratch
- * comes from one PCSF_NOALLOC_SCRATCH_BYTES array compiled into the library
- * (held by every GPU that loads it until exit); a batch that does not fit
- * (more than 32768 regions, more than 131072 column tiles, or more than the
- * area) fails with PCSF_ERANGE.  The first call on a device looks up the
+ * DEVICE pointers owned by the caller; col_offsets is a host array.  The leaf
+ * codes are checked on the device first: a code above PCSF_MARGINALIZE, or a
+ * NULL d_leaves with columns to read, fails with PCSF_EINVAL.  The values are
+ * those pcsf_lpr returns on the same engine (same kernels, summation and P(t)
+ * formation); engines made with PCSF_TC_DIRECT are refused with PCSF_EINVAL.
+ * Scratch comes from one PCSF_NOALLOC_SCRATCH_BYTES array compiled into the
+ * library (held by every GPU that loads it until exit); a batch that does not
+ * fit (more than 32768 regions, more than 131072 column tiles, or more than
+ * the area) fails with PCSF_ERANGE.  The first call on a device looks up the
  * array's device address, so make it before any stream capture.  Calls share
  * the area: calls that overlap on the GPU, or run concurrently from several
  * host threads, race.  Returns after the results are written. */

@@ -1314,24 +1314,29 @@ static int score_impl(pcsf_engine *e, pcsf_batch *b, int strategy, pcsf_result *
 // ---------------------------------------------------------------------------
 // Read-only view of an engine's device state for pcsf_lpr_noalloc (noalloc.cu).
 
-int pcsf_internal_noalloc_ctx(pcsf_engine *e, int *device, cudaStream_t *stream, int *prec, int *compensated, int *nl,
-                              int *nbr, const double **branch, const SchedNode **sched, int *n_internal, int *nslots,
-                              DevModels *m, int *sm_count, int *prune_grid, int **derr)
+int pcsf_internal_noalloc_ctx(pcsf_engine *e, NoallocCtx *c)
 {
-    *device = e->device;
-    *stream = e->stream;
-    *prec = e->prec;
-    *compensated = e->comp_mode();
-    *nl = e->nl;
-    *nbr = e->nbr;
-    *branch = e->dbranch.p;
-    *sched = e->dsched.p;
-    *n_internal = (int)e->sched.size();
-    *nslots = e->nslots;
-    *m = e->dm;
-    *sm_count = e->sm_count;
-    *prune_grid = e->prune_grid;
-    *derr = e->derr.p;
+    if (!e || !c) return PCSF_EINVAL;
+    if (!e->derr.p || !e->dsched.p || !e->dbranch.p) return e->fail(PCSF_EINVAL, "engine is not initialised");
+    c->device = e->device;
+    c->stream = e->stream;
+    c->prec = e->prec;
+    const bool tcprec = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
+    // pcsf_lpr's returned values: the SIMT kernel with the accurate summation on
+    // tensor-core engines, the engine's own summation otherwise
+    c->comp = tcprec ? e->accurate_comp() : e->comp_mode();
+    c->pt64 = e->pt64;
+    c->tc_direct = e->tc_direct;
+    c->has_models = e->has_models;
+    c->nl = e->nl;
+    c->nbr = e->nbr;
+    c->n_internal = (int)e->sched.size();
+    c->nslots = e->nslots;
+    c->branch = e->dbranch.p;
+    c->sched = e->dsched.p;
+    c->m = e->dm;
+    c->prune_grid = e->prune_grid;
+    c->derr = e->derr.p;
     return PCSF_OK;
 }
 

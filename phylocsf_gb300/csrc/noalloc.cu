@@ -13,12 +13,13 @@
 // The scratch area is a file-scope __device__ array of PCSF_NOALLOC_SCRATCH_BYTES
 // (24 MiB): every GPU that loads the library holds it until the process exits.
 // In host code its name is only a host-side stand-in, so its device address
-// is looked up once per device with cudaGetSymbolAddress (on the first call on
-// that device, with that device current).  That first call should therefore
-// come before any stream capture.  All calls share the one area and it keeps
-// the previous call's contents: the parts that must start at zero are cleared
-// on every call, and calls whose work overlaps on the GPU (from several host
-// threads or engines on one device) race on it -- serialise them.  The host
+// is looked up with cudaGetSymbolAddress on the first call on each device, with
+// that device current (a failed lookup is retried by the next call).  That first
+// call should therefore come before any stream capture.  All calls share the one
+// area and it keeps the previous call's contents: the parts that must start at
+// a known value (the status key, the invalid-code slot, the engine's error flag)
+// are set on every call, and calls whose work overlaps on the GPU (from several
+// host threads or engines on one device) race on it -- serialise them.  The host
 // side uses fixed static arrays for the work list, so concurrent calls from
 // several host threads race there too.
 #include <cmath>
@@ -42,44 +43,51 @@ static Request h_req[NOALLOC_MAX_REGIONS];
 static WorkItem h_wi[NOALLOC_MAX_WORK];
 static int32_t h_wib[NOALLOC_MAX_REGIONS + 1];
 
+static std::mutex g_scratch_mu;
 static void *g_scratch_ptr[NOALLOC_MAX_DEVICES];
-static std::once_flag g_scratch_once[NOALLOC_MAX_DEVICES];
-static cudaError_t g_scratch_err[NOALLOC_MAX_DEVICES];
 
-// Device address of the scratch array on `device` (which must be current).
+// Device address of the scratch array on `device` (which must be current).  Only a
+// successful lookup is kept, so a lookup that failed for a passing reason (a sticky
+// error of earlier work, a call made during stream capture) is tried again next time.
 static cudaError_t scratch_on(int device, unsigned char **out)
 {
     if (device < 0 || device >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
-    std::call_once(g_scratch_once[device], [device] {
-        g_scratch_err[device] = cudaGetSymbolAddress(&g_scratch_ptr[device], g_noalloc_scratch);
-    });
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[device]) {
+        void *p = nullptr;
+        cudaError_t ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (ce != cudaSuccess) {
+            cudaGetLastError();   // do not leave the failed lookup as the thread's last error
+            return ce;
+        }
+        g_scratch_ptr[device] = p;
+    }
     *out = reinterpret_cast<unsigned char *>(g_scratch_ptr[device]);
-    return g_scratch_err[device];
+    return cudaSuccess;
 }
+
+static size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
 
 }  // namespace pcsf
 
 using namespace pcsf;
 
 // Engine internals needed here (defined in engine.cpp).
-int pcsf_internal_noalloc_ctx(pcsf_engine *e, int *device, cudaStream_t *stream, int *prec, int *compensated, int *nl,
-                              int *nbr, const double **branch, const SchedNode **sched, int *n_internal, int *nslots,
-                              DevModels *m, int *sm_count, int *prune_grid, int **derr);
+int pcsf_internal_noalloc_ctx(pcsf_engine *e, NoallocCtx *c);
 int pcsf_internal_fail(pcsf_engine *e, int code, const char *msg);
 
 extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32_t n_regions,
                                 const int64_t *col_offsets, const uint8_t *d_leaves, double *d_lpr, double *d_elpr)
 {
     if (!e) return PCSF_EINVAL;
-    int device, prec, comp, nl, nbr, nint, nslots, smc, pgrid;
-    cudaStream_t s;
-    const double *branch;
-    const SchedNode *sched;
-    DevModels m;
-    int *derr;
-    pcsf_internal_noalloc_ctx(e, &device, &s, &prec, &comp, &nl, &nbr, &branch, &sched, &nint, &nslots, &m, &smc,
-                              &pgrid, &derr);
-    if (cudaSetDevice(device) != cudaSuccess) return pcsf_internal_fail(e, PCSF_ECUDA, "pcsf_lpr_noalloc: cudaSetDevice");
+    NoallocCtx cx;
+    int rc = pcsf_internal_noalloc_ctx(e, &cx);
+    if (rc != PCSF_OK) return rc;
+    if (!cx.has_models) return pcsf_internal_fail(e, PCSF_EINVAL, "pcsf_lpr_noalloc: this engine has no coding / noncoding models");
+    if (cx.tc_direct)
+        return pcsf_internal_fail(e, PCSF_EINVAL, "pcsf_lpr_noalloc: engines made with PCSF_TC_DIRECT are not supported "
+                                                  "(their pcsf_lpr returns tensor-core values)");
+    if (cudaSetDevice(cx.device) != cudaSuccess) return pcsf_internal_fail(e, PCSF_ECUDA, "pcsf_lpr_noalloc: cudaSetDevice");
     if (model < 0 || model > 1) return pcsf_internal_fail(e, PCSF_EINVAL, "pcsf_lpr_noalloc: model must be 0 or 1");
     if (!(rho > 0.0) || !std::isfinite(rho)) return pcsf_internal_fail(e, PCSF_EINVAL, "pcsf_lpr_noalloc: rho must be > 0");
     if (n_regions < 0 || (n_regions > 0 && (!col_offsets || !d_lpr)))
@@ -88,18 +96,24 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
         return pcsf_internal_fail(e, PCSF_ERANGE, "pcsf_lpr_noalloc: more than 32768 regions in one call");
     if (n_regions == 0) return PCSF_OK;
     if (col_offsets[0] != 0) return pcsf_internal_fail(e, PCSF_EINVAL, "pcsf_lpr_noalloc: col_offsets[0] must be 0");
-    // every returned likelihood comes from the SIMT kernels (compensated FP32 on
-    // reduced-precision engines), as pcsf_lpr does
-    const int TC = simt_tile_cols(prec, nslots);
-    const size_t es = prec == PCSF_PREC_FP64 ? 8 : 4;
-    // scratch map: [status key][requests][P set][diag(E) low parts][work items][wi_begin][partials]
-    const size_t off_req = 256;
-    const size_t off_ps = off_req + ((sizeof(Request) * n_regions + sizeof(PSet) + 255) & ~size_t(255));
-    const size_t off_P = off_ps + 256;
-    const size_t pbytes = (size_t)nbr * K2 * es;
-    const size_t off_dlo = off_P + ((pbytes + 255) & ~size_t(255));
+    const int64_t total_cols = col_offsets[n_regions];
+    if (total_cols > 0 && !d_leaves) return pcsf_internal_fail(e, PCSF_EINVAL, "pcsf_lpr_noalloc: d_leaves is NULL");
+    // every returned likelihood comes from the SIMT kernels with the summation pcsf_lpr
+    // uses for its returned values, and from the same P(t) formation
+    const int prec = cx.prec;
+    const int TC = simt_tile_cols(prec, cx.nslots);
     const bool fp32 = prec != PCSF_PREC_FP64;
-    const size_t off_wi = off_dlo + (fp32 ? (((size_t)nbr * K * sizeof(float) + 255) & ~size_t(255)) : 0);
+    const size_t es = fp32 ? 4 : 8;
+    const size_t nbr = (size_t)cx.nbr;
+    // scratch map: [status key, invalid-code slot][requests][P set][P(t) in the arithmetic
+    // type][diag(E) low parts][FP64 staging (PCSF_PT_FP64)][work items][wi_begin][partials]
+    const size_t off_req = 256;
+    const size_t off_ps = off_req + up256(sizeof(Request) * (size_t)n_regions);
+    const size_t off_P = off_ps + 256;
+    const size_t off_dlo = off_P + up256(nbr * K2 * es);
+    const size_t off_stage = off_dlo + (fp32 ? up256(nbr * K * sizeof(float)) : 0);
+    const bool stage64 = fp32 && cx.pt64;
+    const size_t off_wi = off_stage + (stage64 ? up256(nbr * K2 * sizeof(double)) : 0);
     int nwi = 0;
     for (int r = 0; r < n_regions; r++) {
         const int64_t c0 = col_offsets[r], c1 = col_offsets[r + 1];
@@ -113,33 +127,54 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
         }
     }
     h_wib[n_regions] = nwi;
-    const size_t off_wib = off_wi + ((sizeof(WorkItem) * (size_t)nwi + 255) & ~size_t(255));
-    const size_t off_part = off_wib + ((sizeof(int32_t) * (size_t)(n_regions + 1) + 255) & ~size_t(255));
-    const size_t need = off_part + sizeof(double) * 2 * (size_t)std::max(nwi, 1);
+    const size_t off_wib = off_wi + up256(sizeof(WorkItem) * (size_t)nwi);
+    const size_t off_part = off_wib + up256(sizeof(int32_t) * (size_t)(n_regions + 1));
+    const size_t off_elpr = off_part + up256(sizeof(double) * 2 * (size_t)std::max(nwi, 1));
+    const size_t need = off_elpr + (d_elpr ? 0 : sizeof(double) * (size_t)n_regions);
     if (need > NOALLOC_BYTES)
         return pcsf_internal_fail(e, PCSF_ERANGE, "pcsf_lpr_noalloc: batch needs more than the 24 MiB static scratch area");
     unsigned char *sc = nullptr;
-    cudaError_t ce = scratch_on(device, &sc);
+    cudaError_t ce = scratch_on(cx.device, &sc);
     if (ce != cudaSuccess) return pcsf_internal_fail(e, PCSF_ECUDA, "pcsf_lpr_noalloc: cudaGetSymbolAddress failed");
     h_ps[0] = PSet{model, 0, rho};
     int32_t *d_status = reinterpret_cast<int32_t *>(sc);
+    unsigned long long *d_badcode = reinterpret_cast<unsigned long long *>(sc + 8);
     Request *d_req = reinterpret_cast<Request *>(sc + off_req);
     PSet *d_ps = reinterpret_cast<PSet *>(sc + off_ps);
     void *d_P = sc + off_P;
     float *d_dlo = fp32 ? reinterpret_cast<float *>(sc + off_dlo) : nullptr;   // as the allocating path
+    double *d_stage = stage64 ? reinterpret_cast<double *>(sc + off_stage) : nullptr;
     WorkItem *d_wi = reinterpret_cast<WorkItem *>(sc + off_wi);
     int32_t *d_wib = reinterpret_cast<int32_t *>(sc + off_wib);
     double *d_part = reinterpret_cast<double *>(sc + off_part);
-    double *d_elpr_out = d_elpr ? d_elpr : d_part + 2 * (size_t)nwi;   // unused tail when no elpr output
-    if (!d_elpr && need + sizeof(double) * n_regions > NOALLOC_BYTES)
-        return pcsf_internal_fail(e, PCSF_ERANGE, "pcsf_lpr_noalloc: batch needs more than the 24 MiB static scratch area");
+    double *d_elpr_out = d_elpr ? d_elpr : reinterpret_cast<double *>(sc + off_elpr);
+    cudaStream_t s = cx.stream;
+    const size_t nbytes = (size_t)total_cols * (size_t)cx.nl;
+    // status key = none, invalid-code slot = none, error flag of timed-out waits cleared
     ce = cudaMemsetAsync(d_status, 0x7f, sizeof(int32_t), s);
-    if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_req, h_req, sizeof(Request) * n_regions, cudaMemcpyHostToDevice, s);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(d_badcode, 0xff, sizeof(unsigned long long), s);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(cx.derr, 0, sizeof(int), s);
+    // the caller's leaf codes are checked on the device, as pcsf_batch_create checks an upload
+    if (ce == cudaSuccess && nbytes) ce = launch_check_codes(d_leaves, nbytes, d_badcode, s);
+    unsigned long long bad = ~0ull;
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&bad, d_badcode, sizeof(bad), cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return pcsf_internal_fail(e, PCSF_ECUDA, cudaGetErrorString(ce));
+    if (bad != ~0ull)
+        return pcsf_internal_fail(e, PCSF_EINVAL, "pcsf_lpr_noalloc: a leaf code is above PCSF_MARGINALIZE (64)");
+    ce = cudaMemcpyAsync(d_req, h_req, sizeof(Request) * n_regions, cudaMemcpyHostToDevice, s);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_ps, h_ps, sizeof(PSet), cudaMemcpyHostToDevice, s);
     if (ce == cudaSuccess && nwi) ce = cudaMemcpyAsync(d_wi, h_wi, sizeof(WorkItem) * nwi, cudaMemcpyHostToDevice, s);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_wib, h_wib, sizeof(int32_t) * (n_regions + 1), cudaMemcpyHostToDevice, s);
-    if (ce == cudaSuccess)
-        ce = launch_pform(prec == PCSF_PREC_FP64, d_ps, 1, branch, nbr, m, d_P, d_status, s, false, nullptr, 0, d_dlo);
+    if (ce == cudaSuccess) {
+        if (stage64) {   // FP64 formation rounded to FP32, as pcsf_lpr on a PCSF_PT_FP64 engine
+            ce = launch_pform(true, d_ps, 1, cx.branch, cx.nbr, cx.m, d_stage, d_status, s);
+            if (ce == cudaSuccess)
+                ce = launch_d2f_rows(d_stage, reinterpret_cast<float *>(d_P), nbr, cx.nbr, nullptr, cx.nl, s, d_dlo);
+        } else {
+            ce = launch_pform(!fp32, d_ps, 1, cx.branch, cx.nbr, cx.m, d_P, d_status, s, false, nullptr, 0, d_dlo);
+        }
+    }
     if (ce == cudaSuccess && nwi) {
         PruneArgs pa{};
         pa.wi = d_wi;
@@ -147,27 +182,25 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
         pa.req = d_req;
         pa.leaves = d_leaves;
         pa.Pbuf = d_P;
-        pa.sched = sched;
-        pa.n_internal = nint;
-        pa.nl = nl;
-        pa.nbr = nbr;
-        pa.nslots = nslots;
-        pa.m = m;
+        pa.sched = cx.sched;
+        pa.n_internal = cx.n_internal;
+        pa.nl = cx.nl;
+        pa.nbr = cx.nbr;
+        pa.nslots = cx.nslots;
+        pa.m = cx.m;
         pa.partials = d_part;
-        pa.dither = prec != PCSF_PREC_FP64;     // as pcsf_lpr, so both give the same values
+        pa.dither = fp32;     // as pcsf_lpr, so both give the same values
         pa.dlo = d_dlo;
-        const bool tcprec = prec == PCSF_PREC_TF32X3 || prec == PCSF_PREC_TF32;
-        ce = launch_prune(prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32, (comp == 0 && tcprec) ? 1 : comp, pa,
-                          s, std::min(pgrid, nwi));
+        ce = launch_prune(fp32 ? PCSF_PREC_FP32 : PCSF_PREC_FP64, cx.comp, pa, s, std::min(cx.prune_grid, nwi));
     }
     if (ce == cudaSuccess) ce = launch_reduce(d_part, d_wib, n_regions, d_lpr, d_elpr_out, s);
     int32_t key = STATUS_NONE;
     int herr = 0;
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(&key, d_status, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
-    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&herr, cx.derr, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
     if (ce != cudaSuccess) return pcsf_internal_fail(e, PCSF_ECUDA, cudaGetErrorString(ce));
-    if (herr) return pcsf_internal_fail(e, PCSF_ECUDA, "pcsf_lpr_noalloc: a tensor-core wait timed out");
+    if (herr) return pcsf_internal_fail(e, PCSF_ECUDA, "pcsf_lpr_noalloc: a device wait timed out");
     if (key >= 0 && key < 0x7f000000) return pcsf_internal_fail(e, key & 15, "pcsf_lpr_noalloc: P(t) formation failed");
     return PCSF_OK;
 }

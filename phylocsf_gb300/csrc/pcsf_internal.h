@@ -179,4 +179,22 @@ bool prune_tc_dual_supported(int nslots, int nl);
 cudaError_t launch_reduce(const double *partials, const int32_t *wi_begin, int nreq, double *out_lpr,
                           double *out_elpr, cudaStream_t s);
 
+// Read-only view of an engine's device state for the allocation-free entry point
+// (noalloc.cu; filled by engine.cpp).
+struct NoallocCtx {
+    int device;
+    cudaStream_t stream;
+    int prec;              // PCSF_PREC_*
+    int comp;              // summation mode of the returned-value kernel (as pcsf_lpr uses it)
+    bool pt64;             // P(t) formed in FP64 and rounded to FP32 (PCSF_PT_FP64)
+    bool tc_direct;        // pcsf_lpr returns tensor-core values (PCSF_TC_DIRECT)
+    bool has_models;
+    int nl, nbr, n_internal, nslots;
+    const double *branch;
+    const SchedNode *sched;
+    DevModels m;
+    int prune_grid;
+    int *derr;             // device error flag of timed-out waits
+};
+
 }  // namespace pcsf

@@ -20,7 +20,9 @@ from . import engine as E
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-PARAMS_DIR = os.path.join(ROOT, "tests", "golden", "params")
+# parameter sets shipped with the package: trees in CamlPaml T order and the coding /
+# noncoding ECMs, parsed from PhyloCSF_Parameters by tests/golden/make_fixtures.py
+PARAMS_DIR = os.path.join(HERE, "params")
 
 
 @dataclass
@@ -34,7 +36,7 @@ class ParamSet:
 
 
 def load_params(name: str, params_dir: Optional[str] = None) -> ParamSet:
-    """A parameter set (tree + coding/noncoding ECMs) from the committed fixtures."""
+    """A parameter set (tree + coding/noncoding ECMs) shipped with the package."""
     d = np.load(os.path.join(params_dir or PARAMS_DIR, name + ".npz"))
 
     def full(tri):
@@ -76,10 +78,7 @@ def simulate(ps: ParamSet, lengths: np.ndarray, models: np.ndarray, gap_frac: Op
     """Simulate regions: returns (col_offsets int64[R+1], leaves uint8[total, nl])."""
     lib = E.load_library()
     tree = ps.tree
-    nbr = tree.n - 1
-    t = tree.branch[:nbr] * rho
-    P = np.ascontiguousarray(np.stack([p_matrices(ps.S_c, ps.pi_c, t), p_matrices(ps.S_n, ps.pi_n, t)]))
-    prior = np.ascontiguousarray(np.stack([ps.pi_c, ps.pi_n]))
+    P, prior = simulation_inputs(ps, rho)
     offs = np.zeros(len(lengths) + 1, np.int64)
     offs[1:] = np.cumsum(lengths)
     leaves = np.empty((int(offs[-1]), tree.nl), np.uint8)
@@ -109,6 +108,28 @@ def gap_fractions(rng: np.random.Generator, nreg: int, nl: int, lo: float, hi: f
 
 
 @dataclass
+class WorkloadSpec:
+    """A workload before its columns are simulated: region lengths (as column offsets),
+    per-region model (0 coding, 1 noncoding), per (region, species) gap probability and
+    the simulation seed.  Building it needs numpy only."""
+    name: str
+    params: ParamSet
+    col_offsets: np.ndarray
+    models: np.ndarray
+    gap_frac: np.ndarray
+    seed: int
+    strategy: int
+
+    @property
+    def n_regions(self) -> int:
+        return len(self.col_offsets) - 1
+
+    @property
+    def total_cols(self) -> int:
+        return int(self.col_offsets[-1])
+
+
+@dataclass
 class Workload:
     name: str
     params: ParamSet
@@ -126,21 +147,41 @@ class Workload:
         return int(self.col_offsets[-1])
 
 
+def realize(spec: WorkloadSpec) -> Workload:
+    """Simulate the columns of a workload (native, multithreaded; deterministic per column)."""
+    lengths = np.diff(spec.col_offsets)
+    offs, lv = simulate(spec.params, lengths, spec.models, spec.gap_frac, spec.seed)
+    return Workload(spec.name, spec.params, offs, lv, spec.models, spec.strategy)
+
+
+def simulation_inputs(ps: ParamSet, rho: float = 1.0):
+    """What the column simulation draws from: per model the P(t) of every branch at tree
+    scale rho, [2][nbr][64][64], and the root priors [2][64]."""
+    nbr = ps.tree.n - 1
+    t = ps.tree.branch[:nbr] * rho
+    P = np.ascontiguousarray(np.stack([p_matrices(ps.S_c, ps.pi_c, t), p_matrices(ps.S_n, ps.pi_n, t)]))
+    prior = np.ascontiguousarray(np.stack([ps.pi_c, ps.pi_n]))
+    return P, prior
+
+
 def log_uniform_lengths(rng, n, lo, hi):
     return np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi), size=n))).astype(np.int64).clip(lo, hi)
 
 
-def workload_12flies_fixed(seed: int = 0) -> Workload:
+def _offsets(lengths) -> np.ndarray:
+    offs = np.zeros(len(lengths) + 1, np.int64)
+    offs[1:] = np.cumsum(lengths)
+    return offs
+
+
+def spec_12flies_fixed(seed: int = 0) -> WorkloadSpec:
     """One alignment of 300 codons on 12flies from the noncoding ECM, 10% gaps per species; fixed."""
     ps = load_params("12flies")
-    rng = np.random.default_rng(seed)
     gf = np.full((1, ps.tree.nl), 0.10)
-    offs, lv = simulate(ps, np.array([300]), np.array([1]), gf, seed)
-    del rng
-    return Workload("12flies_fixed_1x300", ps, offs, lv, np.array([1]), E.FIXED)
+    return WorkloadSpec("12flies_fixed_1x300", ps, _offsets([300]), np.array([1], np.int32), gf, seed, E.FIXED)
 
 
-def workload_58mammals_mle(n_regions: int = 10000, seed: int = 0) -> Workload:
+def spec_58mammals_mle(n_regions: int = 10000, seed: int = 0) -> WorkloadSpec:
     """58mammals, mle: half coding / half noncoding, lengths log-uniform 50-3000 codons,
     per-species gap+N fraction U(5%,40%), 0-20% of species entirely missing."""
     ps = load_params("58mammals")
@@ -148,11 +189,10 @@ def workload_58mammals_mle(n_regions: int = 10000, seed: int = 0) -> Workload:
     lengths = log_uniform_lengths(rng, n_regions, 50, 3000)
     models = (np.arange(n_regions) % 2).astype(np.int32)    # 0 coding, 1 noncoding
     gf = gap_fractions(rng, n_regions, ps.tree.nl, 0.05, 0.40, 0.20)
-    offs, lv = simulate(ps, lengths, models, gf, seed)
-    return Workload("58mammals_mle_%dregions" % n_regions, ps, offs, lv, models, E.MLE)
+    return WorkloadSpec("58mammals_mle_%dregions" % n_regions, ps, _offsets(lengths), models, gf, seed, E.MLE)
 
 
-def workload_120mammals_fixed(total_cols: int = 2_000_000, seed: int = 0) -> Workload:
+def spec_120mammals_fixed(total_cols: int = 2_000_000, seed: int = 0) -> WorkloadSpec:
     """120mammals at rho = 1: alignments log-uniform 100-5000 codons totalling ~total_cols, 1:1 models."""
     ps = load_params("120mammals")
     rng = np.random.default_rng(seed)
@@ -166,16 +206,30 @@ def workload_120mammals_fixed(total_cols: int = 2_000_000, seed: int = 0) -> Wor
     lengths = np.array(lens, np.int64)
     models = (np.arange(len(lengths)) % 2).astype(np.int32)
     gf = gap_fractions(rng, len(lengths), ps.tree.nl, 0.05, 0.40, 0.0)
-    offs, lv = simulate(ps, lengths, models, gf, seed)
-    return Workload("120mammals_fixed_%dcols" % total_cols, ps, offs, lv, models, E.FIXED)
+    return WorkloadSpec("120mammals_fixed_%dcols" % total_cols, ps, _offsets(lengths), models, gf, seed, E.FIXED)
 
 
-def workload_100vertebrates_mle(n_regions: int = 20000, seed: int = 0) -> Workload:
+def spec_100vertebrates_mle(n_regions: int = 20000, seed: int = 0) -> WorkloadSpec:
     """100vertebrates, mle: lengths log-uniform 30-10000 codons, coding:noncoding 1:3, 5-40% gaps."""
     ps = load_params("100vertebrates")
     rng = np.random.default_rng(seed)
     lengths = log_uniform_lengths(rng, n_regions, 30, 10000)
     models = (rng.random(n_regions) >= 0.25).astype(np.int32)
     gf = gap_fractions(rng, n_regions, ps.tree.nl, 0.05, 0.40, 0.0)
-    offs, lv = simulate(ps, lengths, models, gf, seed)
-    return Workload("100vertebrates_mle_%dregions" % n_regions, ps, offs, lv, models, E.MLE)
+    return WorkloadSpec("100vertebrates_mle_%dregions" % n_regions, ps, _offsets(lengths), models, gf, seed, E.MLE)
+
+
+def workload_12flies_fixed(seed: int = 0) -> Workload:
+    return realize(spec_12flies_fixed(seed))
+
+
+def workload_58mammals_mle(n_regions: int = 10000, seed: int = 0) -> Workload:
+    return realize(spec_58mammals_mle(n_regions, seed))
+
+
+def workload_120mammals_fixed(total_cols: int = 2_000_000, seed: int = 0) -> Workload:
+    return realize(spec_120mammals_fixed(total_cols, seed))
+
+
+def workload_100vertebrates_mle(n_regions: int = 20000, seed: int = 0) -> Workload:
+    return realize(spec_100vertebrates_mle(n_regions, seed))

@@ -8,7 +8,8 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REFERENCE = os.environ.get("PHYLOCSF_REFERENCE", "/root/reference")
+# the mlin/PhyloCSF source tree, for the tests that read its files directly (skipped without it)
+REFERENCE = os.environ.get("PHYLOCSF_REFERENCE", "")
 
 
 def pytest_configure(config):
@@ -18,6 +19,6 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def reference_dir():
-    if not os.path.isdir(os.path.join(REFERENCE, "PhyloCSF_Parameters")):
-        pytest.skip("reference source tree not available")
+    if not REFERENCE or not os.path.isdir(os.path.join(REFERENCE, "PhyloCSF_Parameters")):
+        pytest.skip("PHYLOCSF_REFERENCE does not name the reference source tree")
     return REFERENCE

@@ -2,10 +2,12 @@
 
 Run from the repository root with the mlin/PhyloCSF sources available:
 
-    python tests/golden/make_fixtures.py [/path/to/PhyloCSF]
+    python tests/golden/make_fixtures.py /path/to/PhyloCSF
+    (or set PHYLOCSF_REFERENCE to that path)
 
 Writes (all derived, none copied verbatim):
-  params/<set>.npz    tree in CamlPaml T order (parent, children, branch, labels) parsed
+  phylocsf_gb300/params/<set>.npz
+                      tree in CamlPaml T order (parent, children, branch, labels) parsed
                       from PhyloCSF_Parameters/<set>.nh, and the coding /
                       noncoding ECMs (strict lower triangle of S, pi) parsed
                       from PhyloCSF_Parameters/<set>_{coding,noncoding}.ECM
@@ -36,7 +38,7 @@ EXAMPLES = ["tal-AA.fa", "ALDH2.exon5.fa", "Aldh2.mRNA.fa"]
 
 
 def main(ref: str) -> None:
-    pdir = os.path.join(HERE, "params")
+    pdir = os.path.join(ROOT, "phylocsf_gb300", "params")
     os.makedirs(pdir, exist_ok=True)
     il = np.tril_indices(64, -1)
     for name in PARAM_SETS:
@@ -99,4 +101,7 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PHYLOCSF_REFERENCE", "")
+    if not ref or not os.path.isdir(os.path.join(ref, "PhyloCSF_Parameters")):
+        raise SystemExit("usage: make_fixtures.py /path/to/PhyloCSF (or set PHYLOCSF_REFERENCE)")
+    main(ref)

@@ -7,10 +7,11 @@ import numpy as np
 from oracle import oracle as O
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+PARAMS = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "phylocsf_gb300", "params")
 
 
 def fixture_params(name):
-    d = np.load(os.path.join(GOLDEN, "params", name + ".npz"))
+    d = np.load(os.path.join(PARAMS, name + ".npz"))
 
     def full(tri):
         S = np.zeros((64, 64))

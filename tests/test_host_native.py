@@ -78,6 +78,61 @@ def test_ecm_reader_matches_oracle(reference_dir):
         assert np.array_equal(S, S.T) and S[0, 0] == 0.0
 
 
+def _write_ecm(path, S, pi):
+    """An ECM file in the layout ECM.import_parameters reads (src/ECM.ml:18-72): 63 rows of the
+    strict lower triangle, a blank line, the 64 frequencies, two free lines, 64 codons on lines
+    67-70 in index order."""
+    codons = [O.codon_of_index(i) for i in range(64)]
+    lines = [" ".join(repr(float(S[i, j])) for j in range(i)) for i in range(1, 64)]
+    lines += ["", " ".join(repr(float(x)) for x in pi), "", ""]
+    lines += [" ".join(codons[16 * k:16 * k + 16]) for k in range(4)]
+    path.write_text("\n".join(lines) + "\n")
+
+
+def _newick_of(tree):
+    """Newick text of an oracle tree (left child first; branch lengths in repr, so they parse
+    back exactly)."""
+    def rec(i):
+        if tree.lchild[i] < 0:
+            body = tree.labels[i]
+        else:
+            body = "(" + rec(tree.lchild[i]) + "," + rec(tree.rchild[i]) + ")"
+        return body + (":" + repr(float(tree.branch[i])) if tree.parent[i] >= 0 else "")
+    return rec(len(tree.parent) - 1) + ";"
+
+
+@pytest.mark.parametrize("name", ["12flies", "58mammals", "120mammals"])
+def test_readers_round_trip_shipped_parameters(tmp_path, name):
+    """The native ECM reader and Newick parser read back, bit for bit, files written from the
+    parameter sets shipped with the package, and agree with the oracle's readers."""
+    ps = synth.load_params(name)
+    for m, (S, pi) in enumerate(((ps.S_c, ps.pi_c), (ps.S_n, ps.pi_n))):
+        path = tmp_path / ("%s_%d.ECM" % (name, m))
+        _write_ecm(path, S, pi)
+        Sr, pir = P.read_ecm(str(path))
+        So, pio = O.read_ecm(str(path))
+        assert np.array_equal(Sr, S) and np.array_equal(pir, pi)
+        assert np.array_equal(So, S) and np.array_equal(pio, pi)
+    txt = _newick_of(H.fixture_params(name)[0])
+    t = P.Tree.from_newick(txt)
+    o = O.tree_of_newick(O.parse_newick(txt))
+    nb = ps.tree.n - 1
+    assert np.array_equal(t.parent, ps.tree.parent) and np.array_equal(o.parent, ps.tree.parent)
+    assert np.array_equal(t.branch[:nb], ps.tree.branch[:nb]) and np.array_equal(o.branch[:nb], ps.tree.branch[:nb])
+    assert t.labels[:t.nl] == ps.tree.labels[:t.nl] == o.labels[:o.nl]
+
+
+def test_ecm_reader_rejects_bad_codon_order_written(tmp_path):
+    ps = synth.load_params("12flies")
+    path = tmp_path / "bad.ECM"
+    _write_ecm(path, ps.S_c, ps.pi_c)
+    lines = path.read_text().split("\n")
+    lines[67] = lines[67].replace("AAA AAC", "AAC AAA")
+    path.write_text("\n".join(lines))
+    with pytest.raises(P.EngineError, match="codon order"):
+        P.read_ecm(str(path))
+
+
 def test_ecm_reader_rejects_bad_codon_order(tmp_path, reference_dir):
     src = os.path.join(reference_dir, "PhyloCSF_Parameters", "12flies_coding.ECM")
     lines = open(src).read().split("\n")
