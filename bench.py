@@ -69,8 +69,10 @@ def flops_per_column_tangent(nl: int) -> int:
 
 
 KERNEL_NAMES = {0: "k_prune (SIMT, {prec} returned values)", 1: "k_prune_tc<3> (tcgen05 search)",
-                2: "k_grad (adjoint)", 3: "k_prune_tc_dual (tcgen05 tangent)"}
-KERNEL_KEYS = {0: "simt_prune", 1: "tc_prune", 2: "grad", 3: "tc_tangent"}
+                2: "k_grad (adjoint)", 3: "k_prune_tc_dual (tcgen05 tangent)",
+                4: "k_prune_ff (float-float returned values of long regions)"}
+KERNEL_KEYS = {0: "simt_prune", 1: "tc_prune", 2: "grad", 3: "tc_tangent", 4: "ff_prune"}
+NKINDS = len(KERNEL_KEYS)
 
 
 # ---------------------------------------------------------------- distributed
@@ -415,7 +417,7 @@ def run_ours(args, world, rank, local):
     kname = KERNEL_NAMES[kind].format(prec=args.precision)
     kcols = st["kind_columns"][kind]
     kflops = kcols * {0: flops_per_column, 1: flops_per_column, 2: flops_per_column_grad,
-                      3: flops_per_column_tangent}[kind](nl)
+                      3: flops_per_column_tangent, 4: flops_per_column}[kind](nl)
     kms = st["kind_ms"][kind]
     launches = max(st["kind_launches"][kind], 1)
     achieved_tflops = kflops / (kms / 1000.0) / 1e12 if kms > 0 else 0.0
@@ -424,12 +426,12 @@ def run_ours(args, world, rank, local):
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
     traffic = load_traffic(KERNEL_KEYS[kind])
     traffic_per_launch = (traffic * kcols / launches) if traffic else None
-    shares = {KERNEL_KEYS[k]: st["kind_ms"][k] / args.steps for k in range(4)}
+    shares = {KERNEL_KEYS[k]: st["kind_ms"][k] / args.steps for k in range(NKINDS)}
     shares["pform"] = st["pform_ms"] / args.steps
     kinds = {KERNEL_KEYS[k]: {"launches_per_step": st["kind_launches"][k] / args.steps,
                               "column_evals_per_step": st["kind_columns"][k] / args.steps,
                               "ns_per_column_eval": (1e6 * st["kind_ms"][k] / st["kind_columns"][k]
-                                                     if st["kind_columns"][k] else None)} for k in range(4)}
+                                                     if st["kind_columns"][k] else None)} for k in range(NKINDS)}
 
     line = {"metric": METRIC, "value": value, "unit": "regions/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",

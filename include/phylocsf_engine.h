@@ -116,10 +116,12 @@ typedef struct {
     int64_t prune_launches;
     int64_t pform_launches;
     /* by pruning-kernel kind: 0 SIMT (returned values), 1 tensor core (search),
-     * 2 adjoint gradient, 3 tensor-core tangent (d lpr / d rho for the search) */
-    int64_t kind_launches[4];
-    int64_t kind_columns[4];     /* codon-column evaluations (columns x requests)  */
-    double kind_ms[4];           /* device time (these sum to prune_ms)            */
+     * 2 adjoint gradient, 3 tensor-core tangent (d lpr / d rho for the search),
+     * 4 float-float SIMT (returned values of long regions, and the search
+     * decisions of long regions that the tensor-core values cannot settle) */
+    int64_t kind_launches[5];
+    int64_t kind_columns[5];     /* codon-column evaluations (columns x requests)  */
+    double kind_ms[5];           /* device time (these sum to prune_ms)            */
     int32_t prune_grid;     /* launch configuration (not counters): CTAs of the SIMT pruning kernel, */
     int32_t tc_grid;        /* and of the tensor-core kernel (0 if the engine has none)              */
 } pcsf_stats;
@@ -157,6 +159,21 @@ const char *pcsf_last_error(const pcsf_engine *e);
 
 int pcsf_engine_get_stats(const pcsf_engine *e, pcsf_stats *out);
 int pcsf_engine_reset_stats(pcsf_engine *e);
+
+/* Long regions on FP32 and tensor-core engines: a region whose columns x
+ * (n_leaves - 2) reach `units` takes its returned values -- and the search
+ * decisions that the search values cannot settle -- from the float-float kernel
+ * (FP64 P(t), partials carried as float pairs, ~1e-12 relative to the FP64 path)
+ * instead of the compensated FP32 kernel, whose error grows with the region's
+ * length (about 3e-4 dB at 2,000 codons on a 100-leaf tree).  Default 120000
+ * (2,143 codons on 58 leaves, 1,225 on 100).  0: every returned value from the
+ * float-float kernel.  Ignored by the FP64 engine.  No reference counterpart (the
+ * reference computes in FP64 throughout). */
+int pcsf_engine_set_exact_threshold(pcsf_engine *e, int64_t units);
+
+/* 1 if the engine has the float-float kernel (FP32 and tensor-core engines whose
+ * tree fits its shared memory), else 0. */
+int pcsf_engine_exact_available(const pcsf_engine *e);
 
 /* The CUDA stream (a cudaStream_t) on which the engine launches all of its
  * work, so that callers can time it with events on that stream.  No reference

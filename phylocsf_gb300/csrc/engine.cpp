@@ -162,6 +162,11 @@ struct pcsf_engine {
     HostBuf<int32_t> hwib, hstatus;
     HostBuf<double> hlpr, helpr;
     int prune_grid = 0;
+    int ff_grid = 0;               // CTAs of the float-float kernel (0: the tree does not fit it)
+    // returned values (and the accurate search decisions) of a region come from the
+    // float-float kernel when columns x (n_leaves - 2) reaches this; FP32 and tensor-core
+    // engines only (the FP64 engine is exact already)
+    int64_t exact_min_units = 120000;
     int sm_count = 0;
     DevBuf<int> derr;     // set by a kernel whose bounded wait timed out
     DevBuf<unsigned long long> dbadcode;   // first invalid leaf code of an uploaded batch
@@ -589,6 +594,9 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
         return e->fail(PCSF_EINVAL, "tree needs %zu B shared memory for the gradient", gsmem);
     int gper = std::max(1, std::min(4, (int)(prop.sharedMemPerMultiprocessor / (gsmem + 1024))));
     e->grad_grid = prop.multiProcessorCount * gper;
+    if (e->prec != PCSF_PREC_FP64 &&
+        prune_ff_smem_bytes(e->nslots, e->nl, (int)e->sched.size()) <= (size_t)prop.sharedMemPerBlockOptin)
+        e->ff_grid = prop.multiProcessorCount * std::max(1, prune_ff_ctas_per_sm(e->nslots, e->nl, (int)e->sched.size()));
     // P(t) buffer: up to 16 GiB, at most a quarter of free memory.  A round of the
     // search forms one P set per active fit (20,000 fits x 3.6 MB for 58 leaves), so
     // the chunk size sets how many launch pairs (P(t), pruning) a round takes and how
@@ -623,9 +631,11 @@ struct DynGrad {
     const void *Qrow, *Umat, *Bdot;
 };
 
+// exact: the float-float kernel (FP64 P(t), ~1e-12 relative) instead of the FP32 one, on
+// FP32 and tensor-core engines whose tree fits it; implies accurate.
 static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &reqs_in, std::vector<Eval> &out,
                     std::vector<double> *grad = nullptr, bool accurate = false, const DevModels *dyn = nullptr,
-                    std::vector<double> *drho = nullptr, const DynGrad *dg = nullptr)
+                    std::vector<double> *drho = nullptr, const DynGrad *dg = nullptr, bool exact = false)
 {
     const int nreq = (int)reqs_in.size();
     out.assign(nreq, Eval{0.0, 0.0, PCSF_OK});
@@ -634,17 +644,21 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     const int npar = (grad && dg) ? 2 : 0;
     const int gstride = e->nbr + npar;
     if (dyn) accurate = true;
+    const bool ff = exact && !dyn && !grad && !drho && e->prec != PCSF_PREC_FP64 && e->ff_grid > 0;
+    if (ff) accurate = true;
     const DevModels dmv = dyn ? *dyn : e->dm;
     if (drho && (grad || dyn || accurate || !e->dual_ok))
         return e->fail(PCSF_EINVAL, "d lpr / d rho by the tangent pass needs a tensor-core engine and a tree of <= 4 slots");
     const bool tc = (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32) && !accurate;
     // the gradient always runs the SIMT adjoint kernel (64-column tiles in FP32)
     const int TC = grad ? (e->prec == PCSF_PREC_FP64 ? 32 : 64)
-                        : !tc ? simt_tile_cols(e->prec, e->nslots) : prune_tile_cols(e->prec);
+                        : ff ? ff_tile_cols() : !tc ? simt_tile_cols(e->prec, e->nslots) : prune_tile_cols(e->prec);
     const int comp = (accurate && (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32)) ? e->accurate_comp()
                                                                                               : e->comp_mode();
 
-    const int kind = drho ? 3 : grad ? 2 : tc ? 1 : 0;
+    const int kind = drho ? 3 : grad ? 2 : tc ? 1 : ff ? 4 : 0;
+    // FP64 P sets are twice the size of FP32 ones: half as many per chunk
+    const size_t chunk_psets = ff ? std::max<size_t>(1, e->pbuf_psets / 2) : e->pbuf_psets;
     int64_t kind_cols = 0;
     // work items, P-set dedup and chunking (at most pbuf_psets distinct P sets per chunk)
     std::vector<Request> reqs(reqs_in);
@@ -661,7 +675,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         }
     };
     std::unordered_map<std::pair<int, uint64_t>, int, PsKeyHash> cur;
-    cur.reserve(std::min<size_t>((size_t)nreq, e->pbuf_psets) * 2);
+    cur.reserve(std::min<size_t>((size_t)nreq, chunk_psets) * 2);
     wis.reserve((size_t)nreq * 8);
     chunk_req_begin.push_back(0);
     chunk_ps_begin.push_back(0);
@@ -673,7 +687,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         auto key = std::make_pair(q.model, bits);
         auto it = cur.find(key);
         if (it == cur.end()) {
-            if (cur.size() == e->pbuf_psets) {
+            if (cur.size() == chunk_psets) {
                 chunk_req_begin.push_back(r);
                 chunk_ps_begin.push_back((int)psets.size());
                 cur.clear();
@@ -725,16 +739,16 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         CK(e->ddrho.reserve(nreq), "cudaMalloc");
         CK(e->ddscr.reserve(nreq), "cudaMalloc");
     }
-    size_t pset_bytes = (size_t)e->nbr * K2 * (e->prec == PCSF_PREC_FP64 ? 8 : 4);
+    size_t pset_bytes = (size_t)e->nbr * K2 * (e->prec == PCSF_PREC_FP64 || ff ? 8 : 4);
     size_t max_chunk_ps = 0;
     for (size_t c = 0; c + 1 < chunk_ps_begin.size(); c++)
         max_chunk_ps = std::max<size_t>(max_chunk_ps, chunk_ps_begin[c + 1] - chunk_ps_begin[c]);
     CK(e->Pbuf.reserve(max_chunk_ps * pset_bytes), "cudaMalloc P(t) buffer");
     // low parts of diag(E) for the SIMT FP32 kernel (not for the tensor-core search)
-    const bool want_dlo = e->prec != PCSF_PREC_FP64 && !tc && !grad;
+    const bool want_dlo = e->prec != PCSF_PREC_FP64 && !tc && !grad && !ff;
     if (want_dlo) CK(e->Dlo.reserve(max_chunk_ps * (size_t)e->nbr * K), "cudaMalloc P(t) diagonal buffer");
     float *dlo = want_dlo ? e->Dlo.p : nullptr;
-    const bool stage64 = (dyn || e->pt64) && e->prec != PCSF_PREC_FP64;   // FP64 formation, then FP32 storage
+    const bool stage64 = (dyn || e->pt64) && e->prec != PCSF_PREC_FP64 && !ff;   // FP64 formation, then FP32 storage
     if (stage64) CK(e->Pbuf64.reserve(max_chunk_ps * (size_t)e->nbr * K2), "cudaMalloc P(t) staging buffer");
     const int nbop = e->nbr - e->nl;
     const bool want_bop = tc && !grad;
@@ -782,8 +796,8 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
                                reinterpret_cast<float *>(e->Pbuf.p), bop, e->dstatus.p + p0, e->derr.p, s),
                "tensor-core P(t) formation launch");
         } else {
-            CK(launch_pform(e->prec == PCSF_PREC_FP64 || dyn, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, dmv,
-                            e->Pbuf.p, e->dstatus.p + p0, s, false, bop, e->nl, dyn ? nullptr : dlo),
+            CK(launch_pform(e->prec == PCSF_PREC_FP64 || dyn || ff, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, dmv,
+                            e->Pbuf.p, e->dstatus.p + p0, s, false, bop, e->nl, (dyn || ff) ? nullptr : dlo),
                "P(t) formation launch");
         }
         CK(cudaEventRecord(e->ev[1], s), "event");
@@ -836,6 +850,9 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
             int grid = std::min(e->sm_count, std::max(pa.nwi, 1));
             CK(launch_prune_tc_dual(pa, e->dQop.p, e->dbranch.p, e->ddpart.p + 2 * (size_t)wib[r0], e->derr.p, s, grid),
                "tensor-core tangent launch");
+        } else if (ff) {
+            int grid = std::min(e->ff_grid, std::max(pa.nwi, 1));
+            CK(launch_prune_ff(pa, s, grid), "float-float pruning launch");
         } else if (tc) {
             int grid = std::min(e->tc_grid, std::max(pa.nwi, 1));
             CK(launch_prune_tc(e->prec == PCSF_PREC_TF32X3 ? 3 : 1, pa, e->derr.p, s, grid), "tensor-core pruning launch");
@@ -910,14 +927,25 @@ constexpr double DERIV_REL = 1e-4;
 // (measured: the tensor-core error of a difference of nearby points has a standard
 // deviation of ~3.3e-6 nats x sqrt(columns); the band is three of those)
 constexpr double AMBIGUOUS_PER_SQRT_COL = 1e-5;
+// Brent's parabolic step is taken or refused by comparing the parabola's step with
+// half the step before last (the GSL fminimizer's test).  That test moves with the
+// differences of the three f values it interpolates, so near convergence a tensor-core
+// error of a few 1e-4 nats can flip it (seen: 0.966 vs 1.054 of the threshold on a
+// 2,960-codon region), and Brent then follows another path and stops at another point.
+// The test is therefore repeated with every value moved by +-PARABOLA_BAND_PER_SQRT_COL
+// x sqrt(columns); if the outcome can change, the step is computed from accurate values.
+constexpr double PARABOLA_BAND_PER_SQRT_COL = 5e-6;
 
 struct Fit {
     int region = 0, model = 0;
     int64_t ncols = 0;
-    bool deriv = false;   // derivative-assisted small steps (reduced precision)
-    bool accurate_final = false;   // report f(x) from the compensated kernel (tensor-core engines)
+    bool deriv = false;            // derivative-assisted small steps (reduced precision)
+    bool tc_search = false;        // search values from the tensor cores: knife-edge decisions re-decided accurately
+    bool accurate_final = false;   // report f(x) from the accurate values (acache), or xcache when exact
+    bool exact = false;            // report f(x) from the float-float kernel (long regions)
     int prior_kind = 0;            // OmegaModel objectives add a prior on the variable (0: none)
-    std::deque<std::pair<double, Eval>> acache;     // rho -> accurate evaluation
+    std::deque<std::pair<double, Eval>> acache;     // rho -> accurate evaluation (compensated FP32 kernel)
+    std::deque<std::pair<double, Eval>> xcache;     // rho -> float-float evaluation (returned value of a long region)
     std::deque<std::pair<double, double>> gcache;   // rho -> d lpr / d rho
     double lo = 1e-2, hi = 10.0, init = 1.0, accuracy = 0.01;
     int maxtries = 250;
@@ -941,19 +969,77 @@ struct Fit {
             if (c.first == r) return &c.second;
         return nullptr;
     }
+    const Eval *geta(double r) const
+    {
+        for (auto &c : acache)
+            if (c.first == r) return &c.second;
+        return nullptr;
+    }
+    const Eval *getx(double r) const
+    {
+        for (auto &c : xcache)
+            if (c.first == r) return &c.second;
+        return nullptr;
+    }
     const double *getg(double r) const
     {
         for (auto &c : gcache)
             if (c.first == r) return &c.second;
         return nullptr;
     }
+    double band() const { return AMBIGUOUS_PER_SQRT_COL * std::sqrt((double)ncols); }
 };
+
+// One Brent proposal (the GSL fminimizer's step) from the state of f and the values
+// fz = F(bx), fw = F(w), fv = F(v) of the minimised function F = -lpr.
+struct Proposal {
+    double u, e_keep, d_keep;
+    bool tried, parabolic;
+};
+static Proposal brent_propose(const Fit &f, double fz, double fw, double fv)
+{
+    // parabolic step through (x, w, v) if acceptable, else golden section; the two
+    // remembered step lengths swap slots between iterations as in the GSL
+    // implementation the reference drives
+    const double z = f.bx;
+    double d = f.e_keep, ee = f.d_keep;
+    const double tol = SQRT_DBL_EPS * std::fabs(z);
+    const double mid = 0.5 * (f.blo + f.bhi);
+    const double left = z - f.blo, right = f.bhi - z;
+    double p = 0.0, q = 0.0, r = 0.0;
+    Proposal out{};
+    if (std::fabs(ee) > tol) {
+        out.tried = true;
+        r = (z - f.w) * (fz - fv);
+        q = (z - f.v) * (fz - fw);
+        p = (z - f.v) * q - (z - f.w) * r;
+        q = 2.0 * (q - r);
+        if (q > 0.0) p = -p;
+        else q = -q;
+        r = ee;
+        ee = d;
+    }
+    if (std::fabs(p) < std::fabs(0.5 * q * r) && p < q * left && p < q * right) {
+        out.parabolic = true;
+        d = p / q;
+        double uu = z + d;
+        if ((uu - f.blo) < 2.0 * tol || (f.bhi - uu) < 2.0 * tol) d = (z < mid) ? tol : -tol;
+    } else {
+        ee = (z < mid) ? (f.bhi - z) : -(z - f.blo);
+        d = GOLDEN * ee;
+    }
+    out.u = (std::fabs(d) >= tol) ? z + d : z + ((d > 0.0) ? tol : -tol);
+    out.e_keep = ee;
+    out.d_keep = d;
+    return out;
+}
 
 // Advance until a value outside the cache is needed (appended to `need`, to
 // `need_grad` for a gradient, or to `need_acc` for an accurate evaluation) or done.
 static double prior_value(int kind, double x);
 
-static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need_grad, std::vector<double> &need_acc)
+static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need_grad, std::vector<double> &need_acc,
+                    std::vector<double> &need_exact)
 {
     auto ask = [&](double r) -> const Eval * {
         const Eval *ev = f.get(r);
@@ -965,6 +1051,11 @@ static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need
         need.push_back(r);
         return nullptr;
     };
+    auto ask_acc = [&](double r) -> const Eval * {
+        const Eval *ev = f.geta(r);
+        if (!ev) need_acc.push_back(r);
+        return ev;
+    };
     auto failed = [&](const Eval *ev) {
         if (ev->status != PCSF_OK) {
             f.status = ev->status;
@@ -972,6 +1063,20 @@ static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need
             return true;
         }
         return false;
+    };
+    // lpr(a) >= lpr(b) (a at least as good as b), given the search's values la, lb at a, b.
+    // On a tensor-core search, a comparison inside the noise band is decided by the
+    // accurate values of both points instead; -1: those values are needed first (asked for).
+    // Points closer than DERIV_REL |a| keep the search's comparison (their difference is
+    // below the accurate kernel's own rounding noise).
+    auto at_least = [&](double a, double la, double b, double lb) -> int {
+        if (!f.tc_search || f.ncols == 0 || a == b || std::fabs(la - lb) > f.band() ||
+            std::fabs(a - b) <= DERIV_REL * std::fabs(a))
+            return la >= lb;
+        const Eval *ea = ask_acc(a), *eb = ask_acc(b);
+        if (!ea || !eb) return -1;
+        if (failed(ea) || failed(eb)) return -2;
+        return ea->lpr >= eb->lpr;
     };
     for (;;) {
         switch (f.phase) {
@@ -989,7 +1094,16 @@ static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need
             break;
         }
         case Fit::FI_LOOP: {
-            if (f.tries < f.maxtries && (f.fx <= f.flo || f.fx <= f.fhi)) {
+            // find_init's test f(x) <= f(lo) || f(x) <= f(hi) (Fit.ml:39-45), knife edges settled accurately
+            bool retry = false;
+            if (f.tries < f.maxtries) {
+                const int nlo = at_least(f.lo, f.flo, f.x, f.fx);
+                const int nhi = at_least(f.hi, f.fhi, f.x, f.fx);
+                if (nlo == -2 || nhi == -2) return;
+                if (nlo < 0 || nhi < 0) return;
+                retry = nlo == 1 || nhi == 1;
+            }
+            if (retry) {
                 // speculatively request the next few restart points of the deterministic stream
                 const double width = std::log(f.hi) - std::log(f.lo);
                 uint64_t s = f.rng;
@@ -1047,36 +1161,32 @@ static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need
             break;
         }
         case Fit::BR_PROPOSE: {
-            // parabolic step through (x, w, v) if acceptable, else golden section;
-            // the two remembered step lengths swap slots between iterations as
-            // in the GSL implementation the reference drives
-            const double z = f.bx, fz = f.bfx;
-            double d = f.e_keep, ee = f.d_keep;
-            const double tol = SQRT_DBL_EPS * std::fabs(z);
-            const double mid = 0.5 * (f.blo + f.bhi);
-            const double left = z - f.blo, right = f.bhi - z;
-            double p = 0.0, q = 0.0, r = 0.0;
-            if (std::fabs(ee) > tol) {
-                r = (z - f.w) * (fz - f.fv);
-                q = (z - f.v) * (fz - f.fw);
-                p = (z - f.v) * q - (z - f.w) * r;
-                q = 2.0 * (q - r);
-                if (q > 0.0) p = -p;
-                else q = -q;
-                r = ee;
-                ee = d;
+            Proposal pr = brent_propose(f, f.bfx, f.fw, f.fv);
+            // Only a parabola through well-separated points is re-decided: a point reached by a
+            // small step carries the first-order value f(x) + f'(x)(u - x), whose difference to
+            // its neighbour is already exact to first order, while any direct evaluation of two
+            // points that close (< DERIV_REL |x| apart) is dominated by rounding noise.
+            const double sep = DERIV_REL * std::fabs(f.bx);
+            const bool separated = std::fabs(f.bx - f.w) > sep && std::fabs(f.bx - f.v) > sep && std::fabs(f.w - f.v) > sep;
+            if (f.tc_search && f.ncols > 0 && pr.tried && separated) {
+                // is the parabolic test within reach of the search values' noise?
+                const double h = PARABOLA_BAND_PER_SQRT_COL * std::sqrt((double)f.ncols);
+                bool amb = false;
+                for (int m = 0; m < 8 && !amb; m++) {
+                    const Proposal pp = brent_propose(f, f.bfx + ((m & 1) ? h : -h), f.fw + ((m & 2) ? h : -h),
+                                                      f.fv + ((m & 4) ? h : -h));
+                    amb = pp.parabolic != pr.parabolic;
+                }
+                if (amb) {
+                    const Eval *az = ask_acc(f.bx), *aw = ask_acc(f.w), *av = ask_acc(f.v);
+                    if (!az || !aw || !av) return;
+                    if (failed(az) || failed(aw) || failed(av)) return;
+                    pr = brent_propose(f, -az->lpr, -aw->lpr, -av->lpr);
+                }
             }
-            if (std::fabs(p) < std::fabs(0.5 * q * r) && p < q * left && p < q * right) {
-                d = p / q;
-                double uu = z + d;
-                if ((uu - f.blo) < 2.0 * tol || (f.bhi - uu) < 2.0 * tol) d = (z < mid) ? tol : -tol;
-            } else {
-                ee = (z < mid) ? (f.bhi - z) : -(z - f.blo);
-                d = GOLDEN * ee;
-            }
-            f.u = (std::fabs(d) >= tol) ? z + d : z + ((d > 0.0) ? tol : -tol);
-            f.e_keep = ee;
-            f.d_keep = d;
+            f.u = pr.u;
+            f.e_keep = pr.e_keep;
+            f.d_keep = pr.d_keep;
             f.phase = Fit::BR_ACCEPT;
             break;
         }
@@ -1084,7 +1194,8 @@ static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need
             double fu;
             bool better;
             const double u = f.u;
-            if (f.deriv && std::fabs(u - f.bx) <= DERIV_REL * std::fabs(f.bx) && f.ncols > 0) {
+            const bool small = f.deriv && std::fabs(u - f.bx) <= DERIV_REL * std::fabs(f.bx) && f.ncols > 0;
+            if (small) {
                 const Eval *bx = f.get(f.bx);
                 const double *g = f.getg(f.bx);
                 if (!bx || !g) {
@@ -1099,23 +1210,12 @@ static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need
                 if (!a) return;
                 if (failed(a)) return;
                 fu = -a->lpr;
-                better = fu <= f.bfx;
                 // search values from the tensor cores: a comparison inside their noise band is
-                // decided by the compensated kernel's values of both points instead (the state
-                // keeps the search values, so later comparisons stay like for like)
-                if (f.accurate_final && f.ncols > 0 &&
-                    std::fabs(fu - f.bfx) <= AMBIGUOUS_PER_SQRT_COL * std::sqrt((double)f.ncols)) {
-                    const Eval *au = nullptr, *ax = nullptr;
-                    for (auto &c : f.acache) {
-                        if (c.first == u) au = &c.second;
-                        if (c.first == f.bx) ax = &c.second;
-                    }
-                    if (!au) need_acc.push_back(u);
-                    if (!ax) need_acc.push_back(f.bx);
-                    if (!au || !ax) return;
-                    if (failed(au) || failed(ax)) return;
-                    better = -au->lpr <= -ax->lpr;
-                }
+                // decided by the accurate values of both points instead (the state keeps the
+                // search values, so later comparisons stay like for like)
+                const int c = at_least(u, -fu, f.bx, -f.bfx);
+                if (c < 0) return;
+                better = c == 1;
             }
             if (better) {
                 if (u < f.bx) { f.bhi = f.bx; f.bfhi = f.bfx; }
@@ -1124,12 +1224,25 @@ static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need
                 f.w = f.bx; f.fw = f.bfx;
                 f.bx = u; f.bfx = fu;
             } else {
+                // which remembered point u replaces: fu <= fw, else fu <= fv (knife edges
+                // settled accurately, except for the first-order values of small steps)
+                bool le_w = fu <= f.fw, le_v = fu <= f.fv;
+                if (!small && f.w != f.bx) {
+                    const int c = at_least(u, -fu, f.w, -f.fw);
+                    if (c < 0) return;
+                    le_w = c == 1;
+                }
+                if (!small && !(le_w || f.w == f.bx) && f.v != f.bx && f.v != f.w) {
+                    const int c = at_least(u, -fu, f.v, -f.fv);
+                    if (c < 0) return;
+                    le_v = c == 1;
+                }
                 if (u < f.bx) { f.blo = u; f.bflo = fu; }
                 else { f.bhi = u; f.bfhi = fu; }
-                if (fu <= f.fw || f.w == f.bx) {
+                if (le_w || f.w == f.bx) {
                     f.v = f.w; f.fv = f.fw;
                     f.w = u; f.fw = fu;
-                } else if (fu <= f.fv || f.v == f.bx || f.v == f.w) {
+                } else if (le_v || f.v == f.bx || f.v == f.w) {
                     f.v = u; f.fv = fu;
                 }
             }
@@ -1144,12 +1257,13 @@ static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need
         case Fit::FINAL: {
             const Eval *a = nullptr;
             if (f.accurate_final && f.ncols > 0) {
-                for (auto &c : f.acache)
-                    if (c.first == f.x) a = &c.second;
-                if (!a) {
-                    need_acc.push_back(f.x);
-                    return;
+                if (f.exact) {
+                    a = f.getx(f.x);
+                    if (!a) need_exact.push_back(f.x);
+                } else {
+                    a = ask_acc(f.x);
                 }
+                if (!a) return;
             } else {
                 a = ask(f.x);
                 if (!a) return;
@@ -1169,14 +1283,47 @@ static void advance(Fit &f, std::vector<double> &need, std::vector<double> &need
 
 static double decibans(double x) { return 10.0 * x / std::log(10.0); }
 
+// Does a region of ncols columns take its returned values from the float-float kernel?
+static bool is_exact(const pcsf_engine *e, int64_t ncols)
+{
+    return e->prec != PCSF_PREC_FP64 && e->ff_grid > 0 && ncols > 0 &&
+           ncols * (int64_t)std::max(e->nl - 2, 1) >= e->exact_min_units;
+}
+
+// Returned values: the float-float kernel for long regions, the engine's accurate
+// kernel (compensated FP32 SIMT; FP64 on the FP64 engine) for the others.
+static int evaluate_returned(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &reqs, std::vector<Eval> &out)
+{
+    std::vector<Request> ra, rx;
+    std::vector<int> ia, ix;
+    for (int r = 0; r < (int)reqs.size(); r++) {
+        const int64_t nc = b->offs[reqs[r].region + 1] - b->offs[reqs[r].region];
+        (is_exact(e, nc) ? rx : ra).push_back(reqs[r]);
+        (is_exact(e, nc) ? ix : ia).push_back(r);
+    }
+    out.assign(reqs.size(), Eval{0.0, 0.0, PCSF_OK});
+    std::vector<Eval> res;
+    if (!ra.empty()) {
+        int rc = evaluate(e, b, ra, res, nullptr, true);
+        if (rc) return rc;
+        for (size_t k = 0; k < ra.size(); k++) out[ia[k]] = res[k];
+    }
+    if (!rx.empty()) {
+        int rc = evaluate(e, b, rx, res, nullptr, true, nullptr, nullptr, nullptr, true);
+        if (rc) return rc;
+        for (size_t k = 0; k < rx.size(); k++) out[ix[k]] = res[k];
+    }
+    return PCSF_OK;
+}
+
 static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
 {
     // PCSF_TRACE_REGION=<r>: print every evaluation of region r's fits to stderr
     const char *tr = std::getenv("PCSF_TRACE_REGION");
     const int trace = tr ? std::atoi(tr) : -1;
-    std::vector<Request> reqs, greqs, areqs;
-    std::vector<std::pair<int, double>> owner, gowner, aowner;
-    std::vector<Eval> res, gres, ares;
+    std::vector<Request> reqs, greqs, areqs, xreqs;
+    std::vector<std::pair<int, double>> owner, gowner, aowner, xowner;
+    std::vector<Eval> res, gres, ares, xres;
     std::vector<double> grad, drho;
     for (;;) {
         reqs.clear();
@@ -1185,13 +1332,16 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
         gowner.clear();
         areqs.clear();
         aowner.clear();
-        std::vector<double> need, needg, needa;     // reused across fits (no allocation per fit)
+        xreqs.clear();
+        xowner.clear();
+        std::vector<double> need, needg, needa, needx;     // reused across fits (no allocation per fit)
         for (int i = 0; i < (int)fits.size(); i++) {
             need.clear();
             needg.clear();
             needa.clear();
-            advance(fits[i], need, needg, needa);
-            for (auto *lst : {&need, &needg, &needa}) {
+            needx.clear();
+            advance(fits[i], need, needg, needa, needx);
+            for (auto *lst : {&need, &needg, &needa, &needx}) {
                 std::sort(lst->begin(), lst->end());
                 lst->erase(std::unique(lst->begin(), lst->end()), lst->end());
             }
@@ -1199,6 +1349,7 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
             for (double r : need) bad |= !(r > 0.0) || !std::isfinite(r);
             for (double r : needg) bad |= !(r > 0.0) || !std::isfinite(r);
             for (double r : needa) bad |= !(r > 0.0) || !std::isfinite(r);
+            for (double r : needx) bad |= !(r > 0.0) || !std::isfinite(r);
             if (bad) {
                 fits[i].status = PCSF_EINVAL;
                 fits[i].phase = Fit::DONE;
@@ -1228,8 +1379,16 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
                 areqs.push_back(q);
                 aowner.push_back({i, r});
             }
+            for (double r : needx) {
+                Request q{};
+                q.region = fits[i].region;
+                q.model = fits[i].model;
+                q.rho = r;
+                xreqs.push_back(q);
+                xowner.push_back({i, r});
+            }
         }
-        if (reqs.empty() && greqs.empty() && areqs.empty()) break;
+        if (reqs.empty() && greqs.empty() && areqs.empty() && xreqs.empty()) break;
         e->stats.rounds += 1;
         if (!reqs.empty()) {
             int rc = evaluate(e, b, reqs, res);
@@ -1245,7 +1404,23 @@ static int run_fits(pcsf_engine *e, pcsf_batch *b, std::vector<Fit> &fits)
             int rc = evaluate(e, b, areqs, ares, nullptr, true);
             if (rc) return rc;
         }
-        for (size_t k = 0; k < areqs.size(); k++) fits[aowner[k].first].acache.push_back({aowner[k].second, ares[k]});
+        if (!xreqs.empty()) {
+            int rc = evaluate(e, b, xreqs, xres, nullptr, true, nullptr, nullptr, nullptr, true);
+            if (rc) return rc;
+        }
+        for (int pass = 0; pass < 2; pass++) {
+            const auto &rq = pass ? xreqs : areqs;
+            const auto &ow = pass ? xowner : aowner;
+            const auto &rs = pass ? xres : ares;
+            for (size_t k = 0; k < rq.size(); k++) {
+                Fit &f = fits[ow[k].first];
+                (pass ? f.xcache : f.acache).push_back({ow[k].second, rs[k]});
+                if (f.region == trace)
+                    std::fprintf(stderr, "trace region %d model %d round %lld accurate%s rho %.17g lpr %.17g | phase %d\n",
+                                 f.region, f.model, (long long)e->stats.rounds, pass ? " (float-float)" : "",
+                                 ow[k].second, rs[k].lpr, (int)f.phase);
+            }
+        }
         for (size_t k = 0; k < reqs.size(); k++) {
             Fit &f = fits[owner[k].first];
             f.cache.push_back({owner[k].second, res[k]});
@@ -1283,7 +1458,9 @@ static int score_impl(pcsf_engine *e, pcsf_batch *b, int strategy, pcsf_result *
             f.model = m;
             f.ncols = b->offs[r + 1] - b->offs[r];
             f.deriv = e->prec != PCSF_PREC_FP64;
-            f.accurate_final = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
+            f.tc_search = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
+            f.exact = is_exact(e, f.ncols);
+            f.accurate_final = f.tc_search || f.exact;
             if (strategy == PCSF_FIXED) {
                 // llr_FixedLik 1.0: a single evaluation at rho = 1
                 f.x = 1.0;
@@ -1306,7 +1483,7 @@ static int score_impl(pcsf_engine *e, pcsf_batch *b, int strategy, pcsf_result *
         o.score = decibans(c.lpr - nf.lpr);
         o.anc_comp_score = decibans(c.elpr - nf.elpr);
         o.evals = (int32_t)(c.cache.size() + nf.cache.size() + c.gcache.size() + nf.gcache.size() + c.acache.size() +
-                            nf.acache.size());
+                            nf.acache.size() + c.xcache.size() + nf.xcache.size());
     }
     return PCSF_OK;
 }
@@ -1336,6 +1513,8 @@ int pcsf_internal_noalloc_ctx(pcsf_engine *e, NoallocCtx *c)
     c->sched = e->dsched.p;
     c->m = e->dm;
     c->prune_grid = e->prune_grid;
+    c->ff_grid = e->prec != PCSF_PREC_FP64 ? e->ff_grid : 0;
+    c->exact_min_units = e->exact_min_units;
     c->derr = e->derr.p;
     return PCSF_OK;
 }
@@ -1731,8 +1910,8 @@ static int omega_impl(pcsf_engine *e, pcsf_batch *b, double omega_h1, double sig
         for (int r = 0; r < nreg; r++) {
             OmegaRegion &R = regs[r];
             while (!R.done) {
-                std::vector<double> need, needg, needa;
-                advance(R.fit, need, needg, needa);
+                std::vector<double> need, needg, needa, needx;
+                advance(R.fit, need, needg, needa, needx);
                 if (R.fit.phase != Fit::DONE) {
                     std::sort(need.begin(), need.end());
                     need.erase(std::unique(need.begin(), need.end()), need.end());
@@ -1991,6 +2170,16 @@ int pcsf_engine_get_stats(const pcsf_engine *e, pcsf_stats *out)
     return PCSF_OK;
 }
 
+int pcsf_engine_set_exact_threshold(pcsf_engine *e, int64_t units)
+{
+    if (!e) return PCSF_EINVAL;
+    if (units < 0) return e->fail(PCSF_EINVAL, "pcsf_engine_set_exact_threshold: units must be >= 0");
+    e->exact_min_units = units;
+    return PCSF_OK;
+}
+
+int pcsf_engine_exact_available(const pcsf_engine *e) { return e && e->ff_grid > 0 ? 1 : 0; }
+
 int pcsf_engine_reset_stats(pcsf_engine *e)
 {
     if (!e) return PCSF_EINVAL;
@@ -2158,7 +2347,7 @@ int pcsf_lpr(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, do
         reqs[r] = Request{r, model, 0, 0, rho[r]};
     }
     std::vector<Eval> res;
-    int rc = evaluate(e, b, reqs, res, nullptr, !e->tc_direct);
+    int rc = e->tc_direct ? evaluate(e, b, reqs, res) : evaluate_returned(e, b, reqs, res);
     if (rc) return rc;
     for (int r = 0; r < b->nreg; r++) {
         lpr[r] = res[r].lpr;

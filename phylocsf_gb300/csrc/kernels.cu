@@ -683,7 +683,8 @@ cudaError_t launch_prune(int prec, int comp, const PruneArgs &a, cudaStream_t s,
 // ---------------------------------------------------------------------------
 // Per-request sums of the work-item partials, in work-item order (deterministic).
 
-__global__ void k_reduce(const double *partials, const int32_t *wi_begin, int nreq, double *out_lpr, double *out_elpr)
+__global__ void k_reduce(const double *partials, const int32_t *wi_begin, int nreq, double *out_lpr, double *out_elpr,
+                         const int32_t *out_index)
 {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nreq) return;
@@ -692,15 +693,16 @@ __global__ void k_reduce(const double *partials, const int32_t *wi_begin, int nr
         sl += partials[2 * (size_t)w];
         se += partials[2 * (size_t)w + 1];
     }
-    out_lpr[r] = sl;
-    out_elpr[r] = se;
+    const int o = out_index ? out_index[r] : r;
+    out_lpr[o] = sl;
+    out_elpr[o] = se;
 }
 
 cudaError_t launch_reduce(const double *partials, const int32_t *wi_begin, int nreq, double *out_lpr,
-                          double *out_elpr, cudaStream_t s)
+                          double *out_elpr, cudaStream_t s, const int32_t *out_index)
 {
     if (nreq <= 0) return cudaSuccess;
-    k_reduce<<<(nreq + 127) / 128, 128, 0, s>>>(partials, wi_begin, nreq, out_lpr, out_elpr);
+    k_reduce<<<(nreq + 127) / 128, 128, 0, s>>>(partials, wi_begin, nreq, out_lpr, out_elpr, out_index);
     return cudaGetLastError();
 }
 

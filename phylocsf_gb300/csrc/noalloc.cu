@@ -42,6 +42,7 @@ static PSet h_ps[1];
 static Request h_req[NOALLOC_MAX_REGIONS];
 static WorkItem h_wi[NOALLOC_MAX_WORK];
 static int32_t h_wib[NOALLOC_MAX_REGIONS + 1];
+static int32_t h_out[NOALLOC_MAX_REGIONS];   // request -> region (short regions first, then long ones)
 
 static std::mutex g_scratch_mu;
 static void *g_scratch_ptr[NOALLOC_MAX_DEVICES];
@@ -98,35 +99,52 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
     if (col_offsets[0] != 0) return pcsf_internal_fail(e, PCSF_EINVAL, "pcsf_lpr_noalloc: col_offsets[0] must be 0");
     const int64_t total_cols = col_offsets[n_regions];
     if (total_cols > 0 && !d_leaves) return pcsf_internal_fail(e, PCSF_EINVAL, "pcsf_lpr_noalloc: d_leaves is NULL");
-    // every returned likelihood comes from the SIMT kernels with the summation pcsf_lpr
-    // uses for its returned values, and from the same P(t) formation
+    // every returned likelihood comes from the kernels pcsf_lpr uses for it: the SIMT
+    // kernel with pcsf_lpr's summation and P(t) formation, or -- for a region whose
+    // columns x (n_leaves - 2) reach the engine's threshold -- the float-float kernel on
+    // the FP64 P(t)
     const int prec = cx.prec;
     const int TC = simt_tile_cols(prec, cx.nslots);
+    const int TCX = ff_tile_cols();
     const bool fp32 = prec != PCSF_PREC_FP64;
     const size_t es = fp32 ? 4 : 8;
     const size_t nbr = (size_t)cx.nbr;
-    // scratch map: [status key, invalid-code slot][requests][P set][P(t) in the arithmetic
-    // type][diag(E) low parts][FP64 staging (PCSF_PT_FP64)][work items][wi_begin][partials]
+    auto is_long = [&](int64_t nc) {
+        return cx.ff_grid > 0 && nc > 0 && nc * (int64_t)std::max(cx.nl - 2, 1) >= cx.exact_min_units;
+    };
+    // requests: the short regions first, then the long ones; work items contiguous per request
+    int nreq = 0, nwi = 0, nws = 0;
+    bool any_short = false, any_long = false;
+    for (int pass = 0; pass < 2; pass++) {
+        for (int r = 0; r < n_regions; r++) {
+            const int64_t c0 = col_offsets[r], c1 = col_offsets[r + 1];
+            if (c1 < c0) return pcsf_internal_fail(e, PCSF_EINVAL, "pcsf_lpr_noalloc: col_offsets not non-decreasing");
+            if (is_long(c1 - c0) != (pass == 1)) continue;
+            (pass ? any_long : any_short) = true;
+            const int tc = pass ? TCX : TC;
+            h_req[nreq] = Request{r, model, 0, (uint32_t)c0, rho};
+            h_out[nreq] = r;
+            h_wib[nreq] = nwi;
+            for (int64_t c = c0; c < c1; c += tc) {
+                if (nwi >= NOALLOC_MAX_WORK)
+                    return pcsf_internal_fail(e, PCSF_ERANGE, "pcsf_lpr_noalloc: more than 131072 column tiles in one call");
+                h_wi[nwi++] = WorkItem{nreq, (int32_t)std::min<int64_t>(tc, c1 - c), c};
+            }
+            nreq++;
+        }
+        if (pass == 0) nws = nwi;
+    }
+    h_wib[nreq] = nwi;
+    // scratch map: [status key, invalid-code slot][requests][request -> region][P set][P(t) in the
+    // arithmetic type][diag(E) low parts][FP64 P(t)][work items][wi_begin][partials][elpr]
+    const bool stage64 = fp32 && ((cx.pt64 && any_short) || any_long);   // FP64 formation needed
     const size_t off_req = 256;
-    const size_t off_ps = off_req + up256(sizeof(Request) * (size_t)n_regions);
+    const size_t off_out = off_req + up256(sizeof(Request) * (size_t)n_regions);
+    const size_t off_ps = off_out + up256(sizeof(int32_t) * (size_t)n_regions);
     const size_t off_P = off_ps + 256;
     const size_t off_dlo = off_P + up256(nbr * K2 * es);
     const size_t off_stage = off_dlo + (fp32 ? up256(nbr * K * sizeof(float)) : 0);
-    const bool stage64 = fp32 && cx.pt64;
     const size_t off_wi = off_stage + (stage64 ? up256(nbr * K2 * sizeof(double)) : 0);
-    int nwi = 0;
-    for (int r = 0; r < n_regions; r++) {
-        const int64_t c0 = col_offsets[r], c1 = col_offsets[r + 1];
-        if (c1 < c0) return pcsf_internal_fail(e, PCSF_EINVAL, "pcsf_lpr_noalloc: col_offsets not non-decreasing");
-        h_req[r] = Request{r, model, 0, (uint32_t)c0, rho};
-        h_wib[r] = nwi;
-        for (int64_t c = c0; c < c1; c += TC) {
-            if (nwi >= NOALLOC_MAX_WORK)
-                return pcsf_internal_fail(e, PCSF_ERANGE, "pcsf_lpr_noalloc: more than 131072 column tiles in one call");
-            h_wi[nwi++] = WorkItem{r, (int32_t)std::min<int64_t>(TC, c1 - c), c};
-        }
-    }
-    h_wib[n_regions] = nwi;
     const size_t off_wib = off_wi + up256(sizeof(WorkItem) * (size_t)nwi);
     const size_t off_part = off_wib + up256(sizeof(int32_t) * (size_t)(n_regions + 1));
     const size_t off_elpr = off_part + up256(sizeof(double) * 2 * (size_t)std::max(nwi, 1));
@@ -140,6 +158,7 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
     int32_t *d_status = reinterpret_cast<int32_t *>(sc);
     unsigned long long *d_badcode = reinterpret_cast<unsigned long long *>(sc + 8);
     Request *d_req = reinterpret_cast<Request *>(sc + off_req);
+    int32_t *d_out = reinterpret_cast<int32_t *>(sc + off_out);
     PSet *d_ps = reinterpret_cast<PSet *>(sc + off_ps);
     void *d_P = sc + off_P;
     float *d_dlo = fp32 ? reinterpret_cast<float *>(sc + off_dlo) : nullptr;   // as the allocating path
@@ -162,38 +181,46 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
     if (ce != cudaSuccess) return pcsf_internal_fail(e, PCSF_ECUDA, cudaGetErrorString(ce));
     if (bad != ~0ull)
         return pcsf_internal_fail(e, PCSF_EINVAL, "pcsf_lpr_noalloc: a leaf code is above PCSF_MARGINALIZE (64)");
-    ce = cudaMemcpyAsync(d_req, h_req, sizeof(Request) * n_regions, cudaMemcpyHostToDevice, s);
+    ce = cudaMemcpyAsync(d_req, h_req, sizeof(Request) * nreq, cudaMemcpyHostToDevice, s);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_out, h_out, sizeof(int32_t) * nreq, cudaMemcpyHostToDevice, s);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_ps, h_ps, sizeof(PSet), cudaMemcpyHostToDevice, s);
     if (ce == cudaSuccess && nwi) ce = cudaMemcpyAsync(d_wi, h_wi, sizeof(WorkItem) * nwi, cudaMemcpyHostToDevice, s);
-    if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_wib, h_wib, sizeof(int32_t) * (n_regions + 1), cudaMemcpyHostToDevice, s);
-    if (ce == cudaSuccess) {
-        if (stage64) {   // FP64 formation rounded to FP32, as pcsf_lpr on a PCSF_PT_FP64 engine
-            ce = launch_pform(true, d_ps, 1, cx.branch, cx.nbr, cx.m, d_stage, d_status, s);
-            if (ce == cudaSuccess)
-                ce = launch_d2f_rows(d_stage, reinterpret_cast<float *>(d_P), nbr, cx.nbr, nullptr, cx.nl, s, d_dlo);
-        } else {
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_wib, h_wib, sizeof(int32_t) * (nreq + 1), cudaMemcpyHostToDevice, s);
+    if (ce == cudaSuccess && stage64) ce = launch_pform(true, d_ps, 1, cx.branch, cx.nbr, cx.m, d_stage, d_status, s);
+    if (ce == cudaSuccess && any_short) {
+        if (fp32 && cx.pt64)   // FP64 formation rounded to FP32, as pcsf_lpr on a PCSF_PT_FP64 engine
+            ce = launch_d2f_rows(d_stage, reinterpret_cast<float *>(d_P), nbr, cx.nbr, nullptr, cx.nl, s, d_dlo);
+        else
             ce = launch_pform(!fp32, d_ps, 1, cx.branch, cx.nbr, cx.m, d_P, d_status, s, false, nullptr, 0, d_dlo);
-        }
     }
-    if (ce == cudaSuccess && nwi) {
-        PruneArgs pa{};
+    PruneArgs pa{};
+    pa.req = d_req;
+    pa.leaves = d_leaves;
+    pa.sched = cx.sched;
+    pa.n_internal = cx.n_internal;
+    pa.nl = cx.nl;
+    pa.nbr = cx.nbr;
+    pa.nslots = cx.nslots;
+    pa.m = cx.m;
+    if (ce == cudaSuccess && nws) {
         pa.wi = d_wi;
-        pa.nwi = nwi;
-        pa.req = d_req;
-        pa.leaves = d_leaves;
+        pa.nwi = nws;
         pa.Pbuf = d_P;
-        pa.sched = cx.sched;
-        pa.n_internal = cx.n_internal;
-        pa.nl = cx.nl;
-        pa.nbr = cx.nbr;
-        pa.nslots = cx.nslots;
-        pa.m = cx.m;
         pa.partials = d_part;
         pa.dither = fp32;     // as pcsf_lpr, so both give the same values
         pa.dlo = d_dlo;
-        ce = launch_prune(fp32 ? PCSF_PREC_FP32 : PCSF_PREC_FP64, cx.comp, pa, s, std::min(cx.prune_grid, nwi));
+        ce = launch_prune(fp32 ? PCSF_PREC_FP32 : PCSF_PREC_FP64, cx.comp, pa, s, std::min(cx.prune_grid, nws));
     }
-    if (ce == cudaSuccess) ce = launch_reduce(d_part, d_wib, n_regions, d_lpr, d_elpr_out, s);
+    if (ce == cudaSuccess && nwi > nws) {
+        pa.wi = d_wi + nws;
+        pa.nwi = nwi - nws;
+        pa.Pbuf = d_stage;
+        pa.partials = d_part + 2 * (size_t)nws;
+        pa.dither = 0;
+        pa.dlo = nullptr;
+        ce = launch_prune_ff(pa, s, std::min(cx.ff_grid, nwi - nws));
+    }
+    if (ce == cudaSuccess) ce = launch_reduce(d_part, d_wib, nreq, d_lpr, d_elpr_out, s, d_out);
     int32_t key = STATUS_NONE;
     int herr = 0;
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(&key, d_status, sizeof(int32_t), cudaMemcpyDeviceToHost, s);

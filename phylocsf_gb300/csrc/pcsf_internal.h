@@ -176,8 +176,17 @@ size_t prune_tc_dual_smem_bytes(int nl, int nint);
 bool prune_tc_dual_supported(int nslots, int nl);
 
 // Sum the partials of each request's contiguous work items in fixed order.
+// out_index (may be null): request r's sums go to out_*[out_index[r]] instead of out_*[r].
 cudaError_t launch_reduce(const double *partials, const int32_t *wi_begin, int nreq, double *out_lpr,
-                          double *out_elpr, cudaStream_t s);
+                          double *out_elpr, cudaStream_t s, const int32_t *out_index = nullptr);
+
+// Float-float SIMT pruning (ff_kernels.cu): returned values that agree with the FP64
+// path to ~1e-12 relative.  Pbuf holds FP64 E^T sets (the FP64 P(t) formation's output);
+// tiles of ff_tile_cols() columns; partials as k_prune.
+cudaError_t launch_prune_ff(const PruneArgs &a, cudaStream_t s, int grid);
+int ff_tile_cols();
+size_t prune_ff_smem_bytes(int nslots, int nl, int nint);
+int prune_ff_ctas_per_sm(int nslots, int nl, int nint);
 
 // Read-only view of an engine's device state for the allocation-free entry point
 // (noalloc.cu; filled by engine.cpp).
@@ -194,6 +203,8 @@ struct NoallocCtx {
     const SchedNode *sched;
     DevModels m;
     int prune_grid;
+    int ff_grid;           // CTAs of the float-float kernel (0: not available)
+    int64_t exact_min_units;   // regions with columns x (nl - 2) >= this use the float-float kernel
     int *derr;             // device error flag of timed-out waits
 };
 

@@ -78,8 +78,8 @@ class Stats(ctypes.Structure):
                 ("column_branches", ctypes.c_int64), ("rounds", ctypes.c_int64),
                 ("prune_ms", ctypes.c_double), ("pform_ms", ctypes.c_double), ("other_ms", ctypes.c_double),
                 ("prune_launches", ctypes.c_int64), ("pform_launches", ctypes.c_int64),
-                ("kind_launches", ctypes.c_int64 * 4), ("kind_columns", ctypes.c_int64 * 4),
-                ("kind_ms", ctypes.c_double * 4),
+                ("kind_launches", ctypes.c_int64 * 5), ("kind_columns", ctypes.c_int64 * 5),
+                ("kind_ms", ctypes.c_double * 5),
                 ("prune_grid", ctypes.c_int32), ("tc_grid", ctypes.c_int32)]
 
 
@@ -117,6 +117,8 @@ SIGNATURES = {
     "pcsf_pack_regions": ([ctypes.c_int32, _I32, ctypes.c_int32, ctypes.POINTER(ctypes.c_char_p),
                            ctypes.POINTER(ctypes.c_char_p), ctypes.c_int64, ctypes.c_int32, _I32, _I64, _I64, _I64,
                            _U8], ctypes.c_int),
+    "pcsf_engine_set_exact_threshold": ([_VP, ctypes.c_int64], ctypes.c_int),
+    "pcsf_engine_exact_available": ([_VP], ctypes.c_int),
     "pcsf_lpr_noalloc": ([_VP, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, _I64, ctypes.c_void_p, ctypes.c_void_p,
                           ctypes.c_void_p], ctypes.c_int),
     "pcsf_simulate": ([ctypes.c_int32, _I32, ctypes.c_int32, _D, _D, ctypes.c_int32, _I64, _I32, _D, ctypes.c_int32,
@@ -457,6 +459,15 @@ class Engine:
 
     def reset_stats(self):
         _check(self.lib.pcsf_engine_reset_stats(self.handle), self.handle)
+
+    def set_exact_threshold(self, units: int):
+        """Regions with columns x (n_leaves - 2) >= units take their returned values from the
+        float-float kernel (0: all regions)."""
+        _check(self.lib.pcsf_engine_set_exact_threshold(self.handle, int(units)), self.handle)
+
+    @property
+    def exact_available(self) -> bool:
+        return bool(self.lib.pcsf_engine_exact_available(self.handle))
 
 
 # --------------------------------------------------------------------------

@@ -9,8 +9,11 @@ Tolerances (stated per test):
     |d lpr| within max(2.3e-4 nats (= 1e-3 dB),
     5e-9 |lpr|) per model on regions up to 3000 codons for rho in [0.1, 10]
     (the relative term only matters far from the optimum, e.g. rho = 10), fixed-strategy
-    |d score| <= 1e-3 dB.  fp32 (plain summation) carries a downward bias of
-    ~0.3 ulp per contraction; its lpr tolerance is 4e-3 nats.
+    |d score| <= 1e-3 dB, mle |d score| <= 1e-3 dB for every region.  fp32 (plain
+    summation) carries a downward bias of ~0.3 ulp per contraction; its lpr tolerance
+    is 4e-3 nats.
+  - The float-float kernel (returned values of long regions): lpr within 1e-12
+    relative of the FP64 engine.
 """
 import numpy as np
 import pytest
@@ -161,17 +164,40 @@ def test_mle_fp64_follows_oracle_iterates():
         assert g["rho_n"] == pytest.approx(o.rho_n, rel=1e-9)
 
 
-def test_mle_fp32c_close_to_fp64():
-    """The compensated FP32 path against the FP64 path on mle scores (Brent included): |d score| <= 1e-3 dB
-    for at least 95% of regions and <= 5e-3 dB for all."""
-    offs, leaves = _synthetic("58mammals", list(np.random.default_rng(2).integers(50, 1500, size=64)), seed=2)
+@pytest.mark.parametrize("prec", ["fp32c", "fp32b"])
+def test_mle_fp32_close_to_fp64(prec):
+    """The compensated FP32 paths against the FP64 path on mle scores (Brent included): |d score| <= 1e-3 dB
+    for every region."""
+    offs, leaves = _synthetic("58mammals", list(np.random.default_rng(2).integers(50, 3000, size=64)), seed=2)
     a = engine("58mammals", "fp64").score_batch(offs, leaves, P.MLE)
-    b = engine("58mammals", "fp32c").score_batch(offs, leaves, P.MLE)
+    b = engine("58mammals", prec).score_batch(offs, leaves, P.MLE)
     assert (a["status"] == 0).all() and (b["status"] == 0).all()
     d = np.abs(a["score"] - b["score"])
-    assert np.median(d) <= 1e-3
-    assert (d <= 1e-3).mean() >= 0.95, np.sort(d)[-8:]
-    assert d.max() <= 5e-3, np.sort(d)[-8:]
+    assert d.max() <= 1e-3, np.sort(d)[-8:]
+
+
+@pytest.mark.parametrize("name", ["12flies", "58mammals", "100vertebrates", "120mammals"])
+@pytest.mark.parametrize("prec", ["fp32b", "tf32x3b"])
+def test_float_float_kernel_matches_fp64(name, prec):
+    """The float-float kernel (every region forced onto it) against the FP64 engine at fixed rho:
+    lpr and elpr within 1e-12 relative (measured: below 1e-15)."""
+    e = engine(name, prec)
+    if not e.exact_available:
+        pytest.skip("tree does not fit the float-float kernel")
+    e64 = engine(name, "fp64")
+    offs, leaves = _synthetic(name, [1, 31, 32, 33, 300, 1000], seed=23)
+    b, b64 = e.batch(offs, leaves), e64.batch(offs, leaves)
+    e.set_exact_threshold(0)
+    try:
+        for model in (0, 1):
+            for rho in (0.05, 1.0, 4.0):
+                l, el, st = e.lpr(b, model, rho)
+                l64, el64, st64 = e64.lpr(b64, model, rho)
+                assert (st == 0).all() and (st64 == 0).all()
+                assert np.all(np.abs(l - l64) <= 1e-12 * np.abs(l64) + 1e-12), (model, rho, l - l64)
+                assert np.all(np.abs(el - el64) <= 1e-12 * np.abs(el64) + 1e-12), (model, rho, el - el64)
+    finally:
+        e.set_exact_threshold(120000)
 
 
 @pytest.mark.parametrize("prec", PRECS)
