@@ -165,8 +165,8 @@ int pcsf_engine_reset_stats(pcsf_engine *e);
  * decisions that the search values cannot settle -- from the float-float kernel
  * (FP64 P(t), partials carried as float pairs, ~1e-12 relative to the FP64 path)
  * instead of the compensated FP32 kernel, whose error grows with the region's
- * length (about 3e-4 dB at 2,000 codons on a 100-leaf tree).  Default 120000
- * (2,143 codons on 58 leaves, 1,225 on 100).  0: every returned value from the
+ * length (about 1.9e-9 dB per column x internal node: 3e-4 dB at 2,000 codons on a
+ * 100-leaf tree).  Default 150000 (2,679 codons on 58 leaves, 1,531 on 100).  0: every returned value from the
  * float-float kernel.  Ignored by the FP64 engine.  No reference counterpart (the
  * reference computes in FP64 throughout). */
 int pcsf_engine_set_exact_threshold(pcsf_engine *e, int64_t units);

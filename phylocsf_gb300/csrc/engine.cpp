@@ -166,7 +166,7 @@ struct pcsf_engine {
     // returned values (and the accurate search decisions) of a region come from the
     // float-float kernel when columns x (n_leaves - 2) reaches this; FP32 and tensor-core
     // engines only (the FP64 engine is exact already)
-    int64_t exact_min_units = 120000;
+    int64_t exact_min_units = 150000;
     int sm_count = 0;
     DevBuf<int> derr;     // set by a kernel whose bounded wait timed out
     DevBuf<unsigned long long> dbadcode;   // first invalid leaf code of an uploaded batch
@@ -657,8 +657,8 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
                                                                                               : e->comp_mode();
 
     const int kind = drho ? 3 : grad ? 2 : tc ? 1 : ff ? 4 : 0;
-    // FP64 P sets are twice the size of FP32 ones: half as many per chunk
-    const size_t chunk_psets = ff ? std::max<size_t>(1, e->pbuf_psets / 2) : e->pbuf_psets;
+    // a float-float P set (8 B per entry) and its FP64 staging take four times an FP32 one
+    const size_t chunk_psets = ff ? std::max<size_t>(1, e->pbuf_psets / 4) : e->pbuf_psets;
     int64_t kind_cols = 0;
     // work items, P-set dedup and chunking (at most pbuf_psets distinct P sets per chunk)
     std::vector<Request> reqs(reqs_in);
@@ -749,7 +749,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     if (want_dlo) CK(e->Dlo.reserve(max_chunk_ps * (size_t)e->nbr * K), "cudaMalloc P(t) diagonal buffer");
     float *dlo = want_dlo ? e->Dlo.p : nullptr;
     const bool stage64 = (dyn || e->pt64) && e->prec != PCSF_PREC_FP64 && !ff;   // FP64 formation, then FP32 storage
-    if (stage64) CK(e->Pbuf64.reserve(max_chunk_ps * (size_t)e->nbr * K2), "cudaMalloc P(t) staging buffer");
+    if (stage64 || ff) CK(e->Pbuf64.reserve(max_chunk_ps * (size_t)e->nbr * K2), "cudaMalloc P(t) staging buffer");
     const int nbop = e->nbr - e->nl;
     const bool want_bop = tc && !grad;
     if (want_bop) CK(e->Bop.reserve(max_chunk_ps * (size_t)nbop * 2 * K2), "cudaMalloc tensor-core operand buffer");
@@ -785,7 +785,13 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         int r0 = chunk_req_begin[c], r1 = chunk_req_begin[c + 1];
         int p0 = chunk_ps_begin[c], p1 = chunk_ps_begin[c + 1];
         CK(cudaEventRecord(e->ev[0], s), "event");
-        if (stage64) {
+        if (ff) {   // FP64 formation, split into hi / lo floats
+            CK(launch_pform(true, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, dmv, e->Pbuf64.p, e->dstatus.p + p0, s),
+               "P(t) formation launch");
+            CK(launch_split_ff(e->Pbuf64.p, reinterpret_cast<float *>(e->Pbuf.p), (size_t)(p1 - p0) * e->nbr, s),
+               "P(t) split launch");
+            e->stats.kernel_launches += 1;
+        } else if (stage64) {
             CK(launch_pform(true, e->dps.p + p0, p1 - p0, e->dbranch.p, e->nbr, dmv, e->Pbuf64.p, e->dstatus.p + p0, s),
                "P(t) formation launch");
             CK(launch_d2f_rows(e->Pbuf64.p, reinterpret_cast<float *>(e->Pbuf.p), (size_t)(p1 - p0) * e->nbr, e->nbr,

@@ -9,10 +9,11 @@
 // This kernel instead carries every quantity as an unevaluated sum of two floats
 // (hi + lo, ~48 bits):
 //   - E^T = (P - I)^T comes from the FP64 P(t) formation (the FP64 engine's own
-//     matrices, row rule of Q.ml:226-247 applied in FP64) and is split into hi / lo
-//     floats while it is staged into shared memory;
-//   - a leaf child's partial P[a][s] = delta_as + E[a][s] is formed in FP64 and
-//     split (PhyloLik.ml:87-88 with a one-hot leaf);
+//     matrices, row rule of Q.ml:226-247 applied in FP64), split once per P set into
+//     hi / lo floats (k_split_ff) and staged into shared memory asynchronously, one
+//     node ahead;
+//   - a leaf child's partial P[a][s] = delta_as + E[a][s] is formed from the split
+//     entries with an error-free sum (PhyloLik.ml:87-88 with a one-hot leaf);
 //   - an internal child's v = alpha + sum_j E[a][j] alpha[j] (PhyloLik.ml:89-92)
 //     is a compensated dot product: each hi x hi product is split exactly
 //     (TwoProduct by FMA), its hi part is added with TwoSum, and the product
@@ -21,7 +22,12 @@
 //   - each column is rescaled by an exact power of two after every node;
 //   - the root dot with the prior, the log and the tile sums are FP64.
 // The error-free steps use __fadd_rn / __fmul_rn, which the compiler never fuses
-// into an FMA (a fused form would break the exactness the transforms rely on).
+// into an FMA (a fused form would break the exactness the transforms rely on).  The
+// kernel has no FP64 arithmetic outside the root stage: FP64 runs at 1/64 of the FP32
+// rate on this part, and splitting the staged doubles in every tile had cost more
+// than the contractions themselves.
+#include <algorithm>
+
 #include "pcsf_internal.h"
 #include "prune_common.cuh"
 
@@ -50,7 +56,7 @@ __device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &
 struct FFSmem {
     static size_t bytes(int nslots, int nl, int nint)
     {
-        size_t b = sizeof(float) * (4 * (size_t)K2 + 2 * (size_t)nslots * K * FF_TC);   // E^T hi/lo x 2, slots hi/lo
+        size_t b = sizeof(float) * (4 * (size_t)K2 + 2 * (size_t)nslots * K * FF_TC);   // E^T hi/lo x 2 sides, slots hi/lo
         b += sizeof(int) * 2 * FF_TC;                                                   // column maxima (as int bits)
         b += sizeof(int) * FF_TC;                                                       // column exponents
         b += sizeof(SchedNode) * nint;
@@ -60,12 +66,25 @@ struct FFSmem {
     }
 };
 
+// FP64 E^T sets [nmat][K2] -> float-float [nmat][hi K2 | lo K2]: hi = the nearest float,
+// lo = the nearest float to the remainder (together ~48 bits).
+__global__ void k_split_ff(const double *in, float *out, size_t nmat)
+{
+    const size_t n = nmat * K2;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double x = in[i];
+        const float h = (float)x;
+        const size_t m = i / K2, k = i - m * K2;
+        out[m * 2 * K2 + k] = h;
+        out[m * 2 * K2 + K2 + k] = (float)(x - (double)h);
+    }
+}
+
 __global__ void __launch_bounds__(FF_THREADS) k_prune_ff(PruneArgs a)
 {
     extern __shared__ __align__(16) unsigned char ssm[];
-    float *EtH = reinterpret_cast<float *>(ssm);            // [2][K][K]
-    float *EtL = EtH + 2 * K2;                               // [2][K][K]
-    float *slH = EtL + 2 * K2;                               // [nslots][K][TC]
+    float *Et = reinterpret_cast<float *>(ssm);              // [2 sides][hi K2 | lo K2]
+    float *slH = Et + 4 * K2;                                // [nslots][K][TC]
     float *slL = slH + (size_t)a.nslots * K * FF_TC;         // [nslots][K][TC]
     int *colmax = reinterpret_cast<int *>(slL + (size_t)a.nslots * K * FF_TC);   // [2][TC]
     int *cscale = colmax + 2 * FF_TC;                                            // [TC]
@@ -85,9 +104,25 @@ __global__ void __launch_bounds__(FF_THREADS) k_prune_ff(PruneArgs a)
         const WorkItem wi = a.wi[w];
         const Request rq = a.req[wi.request];
         const int md = rq.model;
-        const double *Pbase = reinterpret_cast<const double *>(a.Pbuf) + (size_t)rq.pset * a.nbr * K2;
+        const float *Pbase = reinterpret_cast<const float *>(a.Pbuf) + (size_t)rq.pset * a.nbr * 2 * K2;
         const int ncols = wi.ncols;
         const uint8_t *lg = a.leaves + (size_t)wi.col0 * nl;
+        // the split E^T (hi and lo blocks, 32 KB) of a node's internal children into shared
+        // memory, copied asynchronously one node ahead; leaf children read their rows from
+        // global memory instead
+        auto copy_inner = [&](const SchedNode &nx) {
+            constexpr int NV = 2 * K2 * sizeof(float) / 16;
+#pragma unroll
+            for (int side = 0; side < 2; side++) {
+                if ((side ? nx.rslot : nx.lslot) < 0) continue;
+                const char *src = reinterpret_cast<const char *>(Pbase + (size_t)(side ? nx.rc : nx.lc) * 2 * K2);
+                const uint32_t dst = (uint32_t)__cvta_generic_to_shared(Et + side * 2 * K2);
+                for (int f = tid; f < NV; f += FF_THREADS)
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(dst + 16 * f), "l"(src + 16 * f)
+                                 : "memory");
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
+        };
         __syncthreads();   // previous work item finished with shared memory
         for (int f = tid; f < FF_TC * nl; f += FF_THREADS) {
             const int c = f / nl, l = f - c * nl;
@@ -96,48 +131,41 @@ __global__ void __launch_bounds__(FF_THREADS) k_prune_ff(PruneArgs a)
         for (int f = tid; f < 2 * FF_TC; f += FF_THREADS) colmax[f] = 0;
         for (int f = tid; f < FF_TC; f += FF_THREADS) cscale[f] = 0;
 
+        copy_inner(sched[0]);
         for (int ni = 0; ni < a.n_internal; ni++) {
             const SchedNode sn = sched[ni];
-            // E^T of the internal children, split into hi / lo floats
-            for (int side = 0; side < 2; side++) {
-                if ((side ? sn.rslot : sn.lslot) < 0) continue;
-                const double2 *src = reinterpret_cast<const double2 *>(Pbase + (size_t)(side ? sn.rc : sn.lc) * K2);
-                float2 *dh = reinterpret_cast<float2 *>(EtH + side * K2);
-                float2 *dl = reinterpret_cast<float2 *>(EtL + side * K2);
-                for (int f = tid; f < K2 / 2; f += FF_THREADS) {
-                    const double2 x = __ldg(src + f);
-                    const float hx = (float)x.x, hy = (float)x.y;
-                    dh[f] = make_float2(hx, hy);
-                    dl[f] = make_float2((float)(x.x - (double)hx), (float)(x.y - (double)hy));
-                }
-            }
-            __syncthreads();
+            asm volatile("cp.async.wait_all;" ::: "memory");
+            __syncthreads();   // this node's E^T staged, the previous node's slots written
             float vh[2][4][FF_CPT], vl[2][4][FF_CPT];
 #pragma unroll
             for (int side = 0; side < 2; side++) {
                 const int slot = side ? sn.rslot : sn.lslot;
                 const int child = side ? sn.rc : sn.lc;
                 if (slot < 0) {
-                    // leaf: P[a][s] = delta_as + E[a][s] in FP64, split; 1 for a marginalised leaf
-                    const double *Et = Pbase + (size_t)child * K2;
+                    // leaf: P[a][s] = delta_as + E[a][s] from the split entries; 1 for a marginalised leaf
+                    const float *Eg = Pbase + (size_t)child * 2 * K2;
 #pragma unroll
                     for (int cc = 0; cc < FF_CPT; cc++) {
                         const int s = lvT[child * FF_TC + c0 + cc];
-                        const double *row = Et + (size_t)(s < K ? s : 0) * K + a0;
-                        const double2 r01 = __ldg(reinterpret_cast<const double2 *>(row));
-                        const double2 r23 = __ldg(reinterpret_cast<const double2 *>(row + 2));
-                        const double e4[4] = {r01.x, r01.y, r23.x, r23.y};
+                        const int sr = s < K ? s : 0;
+                        const float4 h4 = __ldg(reinterpret_cast<const float4 *>(Eg + sr * K + a0));
+                        const float4 l4 = __ldg(reinterpret_cast<const float4 *>(Eg + K2 + sr * K + a0));
+                        const float hv[4] = {h4.x, h4.y, h4.z, h4.w}, lv[4] = {l4.x, l4.y, l4.z, l4.w};
 #pragma unroll
                         for (int i = 0; i < 4; i++) {
-                            const double x = (s >= K) ? 1.0 : e4[i] + (a0 + i == s ? 1.0 : 0.0);
-                            const float h = (float)x;
-                            vh[side][i][cc] = h;
-                            vl[side][i][cc] = (float)(x - (double)h);
+                            float h = hv[i], l = lv[i];
+                            if (a0 + i == s) {   // 1 + E_ss: exact sum, then the low part folded in
+                                float t, e;
+                                two_sum(1.0f, h, t, e);
+                                fast_two_sum(t, __fadd_rn(e, l), h, l);
+                            }
+                            vh[side][i][cc] = (s >= K) ? 1.0f : h;
+                            vl[side][i][cc] = (s >= K) ? 0.0f : l;
                         }
                     }
                 } else {
                     // internal: v = alpha + sum_j E[a][j] alpha[j], compensated
-                    const float *Eh = EtH + side * K2, *El = EtL + side * K2;
+                    const float *Eh = Et + side * 2 * K2, *El = Eh + K2;
                     const float *xH = slH + (size_t)slot * K * FF_TC, *xL = slL + (size_t)slot * K * FF_TC;
                     float sh[4][FF_CPT], sl[4][FF_CPT];
 #pragma unroll
@@ -178,6 +206,8 @@ __global__ void __launch_bounds__(FF_THREADS) k_prune_ff(PruneArgs a)
                         }
                 }
             }
+            __syncthreads();   // every thread is past its reads of the E^T buffers and the child slots
+            if (ni + 1 < a.n_internal) copy_inner(sched[ni + 1]);   // E^T buffers are free again
             // alpha = v_l * v_r (float-float product), column maxima of the hi parts
             int *cm = colmax + (ni & 1) * FF_TC;
             int *cm_next = colmax + ((ni + 1) & 1) * FF_TC;
@@ -200,7 +230,7 @@ __global__ void __launch_bounds__(FF_THREADS) k_prune_ff(PruneArgs a)
                 }
                 atomicMax(cm + c0 + cc, __float_as_int(mx));   // non-negative floats order as ints
             }
-            __syncthreads();   // every thread is past its reads of the E^T buffers and the child slots
+            __syncthreads();   // column maxima complete
             float *oH = slH + (size_t)sn.oslot * K * FF_TC, *oL = slL + (size_t)sn.oslot * K * FF_TC;
             int ecol[FF_CPT];
 #pragma unroll
@@ -220,8 +250,8 @@ __global__ void __launch_bounds__(FF_THREADS) k_prune_ff(PruneArgs a)
                 ColStore<float, FF_CPT>::store(oH + (a0 + i) * FF_TC + c0, yh);
                 ColStore<float, FF_CPT>::store(oL + (a0 + i) * FF_TC + c0, yl);
             }
-            __syncthreads();   // slots written before the next node reads them or the E^T buffers are refilled
         }
+        __syncthreads();   // the root's slot written
         // root: z = alpha_root . prior ; elpr term = (alpha_root . prior*log prior) / z, in FP64
         double tl = 0.0, te = 0.0;
         if (tid < FF_TC && tid < ncols) {
@@ -268,6 +298,15 @@ __global__ void __launch_bounds__(FF_THREADS) k_prune_ff(PruneArgs a)
 }  // namespace
 
 int ff_tile_cols() { return FF_TC; }
+
+cudaError_t launch_split_ff(const double *in, float *out, size_t nmat, cudaStream_t s)
+{
+    if (nmat == 0) return cudaSuccess;
+    const size_t n = nmat * K2;
+    const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 4096);
+    k_split_ff<<<blocks, 256, 0, s>>>(in, out, nmat);
+    return cudaGetLastError();
+}
 
 size_t prune_ff_smem_bytes(int nslots, int nl, int nint) { return FFSmem::bytes(nslots, nl, nint); }
 

@@ -136,15 +136,17 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
     }
     h_wib[nreq] = nwi;
     // scratch map: [status key, invalid-code slot][requests][request -> region][P set][P(t) in the
-    // arithmetic type][diag(E) low parts][FP64 P(t)][work items][wi_begin][partials][elpr]
+    // arithmetic type][diag(E) low parts][FP64 P(t)][float-float P(t)][work items][wi_begin][partials][elpr]
     const bool stage64 = fp32 && ((cx.pt64 && any_short) || any_long);   // FP64 formation needed
+    const size_t split_bytes = any_long ? up256(nbr * 2 * K2 * sizeof(float)) : 0;   // float-float P set
     const size_t off_req = 256;
     const size_t off_out = off_req + up256(sizeof(Request) * (size_t)n_regions);
     const size_t off_ps = off_out + up256(sizeof(int32_t) * (size_t)n_regions);
     const size_t off_P = off_ps + 256;
     const size_t off_dlo = off_P + up256(nbr * K2 * es);
     const size_t off_stage = off_dlo + (fp32 ? up256(nbr * K * sizeof(float)) : 0);
-    const size_t off_wi = off_stage + (stage64 ? up256(nbr * K2 * sizeof(double)) : 0);
+    const size_t off_split = off_stage + (stage64 ? up256(nbr * K2 * sizeof(double)) : 0);
+    const size_t off_wi = off_split + split_bytes;
     const size_t off_wib = off_wi + up256(sizeof(WorkItem) * (size_t)nwi);
     const size_t off_part = off_wib + up256(sizeof(int32_t) * (size_t)(n_regions + 1));
     const size_t off_elpr = off_part + up256(sizeof(double) * 2 * (size_t)std::max(nwi, 1));
@@ -163,6 +165,7 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
     void *d_P = sc + off_P;
     float *d_dlo = fp32 ? reinterpret_cast<float *>(sc + off_dlo) : nullptr;   // as the allocating path
     double *d_stage = stage64 ? reinterpret_cast<double *>(sc + off_stage) : nullptr;
+    float *d_split = any_long ? reinterpret_cast<float *>(sc + off_split) : nullptr;
     WorkItem *d_wi = reinterpret_cast<WorkItem *>(sc + off_wi);
     int32_t *d_wib = reinterpret_cast<int32_t *>(sc + off_wib);
     double *d_part = reinterpret_cast<double *>(sc + off_part);
@@ -187,6 +190,7 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
     if (ce == cudaSuccess && nwi) ce = cudaMemcpyAsync(d_wi, h_wi, sizeof(WorkItem) * nwi, cudaMemcpyHostToDevice, s);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_wib, h_wib, sizeof(int32_t) * (nreq + 1), cudaMemcpyHostToDevice, s);
     if (ce == cudaSuccess && stage64) ce = launch_pform(true, d_ps, 1, cx.branch, cx.nbr, cx.m, d_stage, d_status, s);
+    if (ce == cudaSuccess && any_long) ce = launch_split_ff(d_stage, d_split, nbr, s);
     if (ce == cudaSuccess && any_short) {
         if (fp32 && cx.pt64)   // FP64 formation rounded to FP32, as pcsf_lpr on a PCSF_PT_FP64 engine
             ce = launch_d2f_rows(d_stage, reinterpret_cast<float *>(d_P), nbr, cx.nbr, nullptr, cx.nl, s, d_dlo);
@@ -214,7 +218,7 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
     if (ce == cudaSuccess && nwi > nws) {
         pa.wi = d_wi + nws;
         pa.nwi = nwi - nws;
-        pa.Pbuf = d_stage;
+        pa.Pbuf = d_split;
         pa.partials = d_part + 2 * (size_t)nws;
         pa.dither = 0;
         pa.dlo = nullptr;

@@ -181,9 +181,11 @@ cudaError_t launch_reduce(const double *partials, const int32_t *wi_begin, int n
                           double *out_elpr, cudaStream_t s, const int32_t *out_index = nullptr);
 
 // Float-float SIMT pruning (ff_kernels.cu): returned values that agree with the FP64
-// path to ~1e-12 relative.  Pbuf holds FP64 E^T sets (the FP64 P(t) formation's output);
-// tiles of ff_tile_cols() columns; partials as k_prune.
+// path to ~1e-12 relative.  Pbuf holds split E^T sets, per P set [nbr][hi K2 | lo K2]
+// floats, made from the FP64 P(t) formation's output by launch_split_ff; tiles of
+// ff_tile_cols() columns; partials as k_prune.
 cudaError_t launch_prune_ff(const PruneArgs &a, cudaStream_t s, int grid);
+cudaError_t launch_split_ff(const double *in, float *out, size_t nmat, cudaStream_t s);
 int ff_tile_cols();
 size_t prune_ff_smem_bytes(int nslots, int nl, int nint);
 int prune_ff_ctas_per_sm(int nslots, int nl, int nint);

@@ -62,14 +62,14 @@ def test_120mammals_precision(workload, reference, prec, rel_bound, db_bound):
 @pytest.mark.parametrize("prec", ["fp32b", "tf32x3b"])
 def test_long_regions_fixed_rho(prec):
     """Returned values on long 100vertebrates regions (2,000 / 5,000 / 10,000 codons) at fixed rho,
-    against FP64.  Regions at or past the engine's threshold (columns x (n_leaves - 2) >= 120,000,
-    1,225 codons here) take their values from the float-float kernel: |d score| <= 1e-6 dB
-    (measured ~1e-10).  Regions just below it (1,224 codons) stay on the compensated FP32 kernel,
+    against FP64.  Regions at or past the engine's threshold (columns x (n_leaves - 2) >= 150,000,
+    1,531 codons here) take their values from the float-float kernel: |d score| <= 1e-6 dB
+    (measured ~1e-10).  Regions just below it (1,530 codons) stay on the compensated FP32 kernel,
     whose error grows roughly linearly with length (measured max 3.0e-4 / 8.8e-4 / 1.6e-3 dB at
     2,000 / 5,000 / 10,000 codons without the float-float kernel): <= 5e-4 dB."""
     ps = synth.load_params("100vertebrates")
     rng = np.random.default_rng(11)
-    lengths = np.array([2000] * 4 + [5000] * 4 + [10000] * 2 + [1224] * 8)
+    lengths = np.array([2000] * 4 + [5000] * 4 + [10000] * 2 + [1530] * 8)
     models = (rng.random(len(lengths)) >= 0.25).astype(np.int32)
     gf = synth.gap_fractions(rng, len(lengths), ps.tree.nl, 0.05, 0.40, 0.0)
     offs, lv = synth.simulate(ps, lengths, models, gf, 5)
@@ -80,7 +80,7 @@ def test_long_regions_fixed_rho(prec):
         c0, n0 = e64.lpr(b64, 0, rho)[0], e64.lpr(b64, 1, rho)[0]
         c, n = e.lpr(b, 0, rho)[0], e.lpr(b, 1, rho)[0]
         ddb = np.abs(10.0 * ((c - n) - (c0 - n0)) / np.log(10.0))
-        print("%s rho %.1f: float-float regions max %.2e dB; 1,224-codon regions (FP32 kernel) max %.2e dB"
+        print("%s rho %.1f: float-float regions max %.2e dB; 1,530-codon regions (FP32 kernel) max %.2e dB"
               % (prec, rho, ddb[:10].max(), ddb[10:].max()))
         assert ddb[:10].max() <= 1e-6
         assert ddb[10:].max() <= 5e-4
