@@ -229,6 +229,37 @@ int pcsf_lpr(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, do
 int pcsf_grad(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, double *lpr, double *d_branch,
               double *d_rho, int32_t *status);
 
+/* ---------------------------------------------- outside-pass statistics */
+
+/* Expected substitution counts of every branch, summed over each region's columns,
+ * for model m at tree scale rho[r]:
+ *   counts[r][i][a][b] = sum_col beta_p[a] (P_s alpha_s)[a] P_i[a][b] alpha_i[b] / z
+ * (p the parent of node i, s its sibling, P_i = P(rho[r] b_i)).  This is
+ * PhyloLik.add_branch_posteriors (lib/CamlPaml/PhyloLik.ml:140-174) accumulated over
+ * the columns as PhyloEM.collect_sufficient_statistics does (lib/CamlPaml/PhyloEM.ml:14-20).
+ * Each branch's counts sum to the number of columns with z > 0.  counts:
+ * [n_regions][2*n_leaves-2][64][64]; lpr and status ([n_regions]) may be NULL.
+ * Computed in FP64 on the FP64 engine, in FP32 with compensated sums otherwise. */
+int pcsf_branch_counts(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, double *counts, double *lpr,
+                       int32_t *status);
+
+/* Expected log-likelihood of sufficient statistics (PhyloEM.ell,
+ * lib/CamlPaml/PhyloEM.ml:22-73) for model m at tree scale rho: the sum over
+ * branches of counts x log P(rho b_i) over the positive counts, plus the root prior
+ * term from the row sums of the counts of the root's left child.  counts:
+ * [2*n_leaves-2][64][64] (one region's counts from pcsf_branch_counts, or a sum of
+ * several).  P(t) is formed in FP64. */
+int pcsf_ell(pcsf_engine *e, int32_t model, double rho, const double *counts, double *ell);
+
+/* Posterior state distributions of selected nodes at every column of a batch, for
+ * model m at tree scale rho[r] of each region (PhyloLik.node_posterior,
+ * lib/CamlPaml/PhyloLik.ml:127-138): alpha_i[a] beta_i[a] / z for an internal node or
+ * the root, the leaf's own vector (one-hot, or all ones when marginalised) for a
+ * leaf, and zeros where z = 0.  nodes: [n_nodes] in T order; post:
+ * [n_nodes][total_cols][64]; status [n_regions] may be NULL. */
+int pcsf_node_posteriors(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, int32_t n_nodes,
+                         const int32_t *nodes, double *post, int32_t *status);
+
 /* ------------------------------------------------------- allocation-free */
 
 /* Size of the fixed device scratch area behind pcsf_lpr_noalloc. */

@@ -18,7 +18,8 @@ Two layers:
   - pleaves (leaf encoding) ........ src/PhyloCSF.ml:219-246
 
 * ctypes bindings to ``phylocsf_oracle.c`` (the FP64 numeric restatement:
-  Q build, eigendecomposition, P(t), dense pruning, find_init + Brent, LLR).
+  Q build, eigendecomposition, P(t), dense pruning, find_init + Brent, LLR,
+  outside pass, node posteriors, expected branch counts and ELL).
 """
 from __future__ import annotations
 
@@ -478,6 +479,9 @@ def _lib():
                                        ctypes.c_int, I, D, D]
         lib.orc_grad_branches.argtypes = [ctypes.POINTER(_Model), ctypes.POINTER(_Tree), ctypes.c_double,
                                           ctypes.c_int, I, D, D]
+        lib.orc_branch_counts.argtypes = [ctypes.POINTER(_Model), ctypes.POINTER(_Tree), ctypes.c_double,
+                                          ctypes.c_int, I, D, D]
+        lib.orc_ell.argtypes = [ctypes.POINTER(_Model), ctypes.POINTER(_Tree), ctypes.c_double, D, D]
         lib.orc_score_region.argtypes = [ctypes.POINTER(_Model), ctypes.POINTER(_Model), ctypes.POINTER(_Tree),
                                          ctypes.c_int, ctypes.c_int, I, ctypes.POINTER(Result)]
         lib.orc_score_batch.argtypes = [ctypes.POINTER(_Model), ctypes.POINTER(_Model), ctypes.POINTER(_Tree),
@@ -595,6 +599,28 @@ def grad_branches(model: OModel, otree: OTree, rho: float, leaves: np.ndarray) -
     if st:
         raise RuntimeError("orc_grad_branches status %d" % st)
     return lpr.value, g
+
+
+def branch_counts(model: OModel, otree: OTree, rho: float, leaves: np.ndarray) -> Tuple[float, np.ndarray]:
+    """(lpr, expected substitution counts [n-1][k][k] summed over the columns)."""
+    lv = _leaves_c(leaves)
+    lpr = ctypes.c_double()
+    c = np.zeros((otree.tree.n - 1, model.k, model.k))
+    st = _lib().orc_branch_counts(ctypes.byref(model.c), ctypes.byref(otree.c), rho, lv.shape[0], _ip(lv),
+                                  ctypes.byref(lpr), _dp(c))
+    if st:
+        raise RuntimeError("orc_branch_counts status %d" % st)
+    return lpr.value, c
+
+
+def ell(model: OModel, otree: OTree, rho: float, counts: np.ndarray) -> float:
+    """PhyloEM.ell of sufficient statistics counts [n-1][k][k] at tree scale rho."""
+    out = ctypes.c_double()
+    cc = np.ascontiguousarray(counts, np.float64)
+    st = _lib().orc_ell(ctypes.byref(model.c), ctypes.byref(otree.c), rho, _dp(cc), ctypes.byref(out))
+    if st:
+        raise RuntimeError("orc_ell status %d" % st)
+    return out.value
 
 
 FIXED, MLE = 0, 1

@@ -18,6 +18,7 @@
  *   - root posterior, lpr / elpr_anc ........... lib/CamlPaml/PhyloLik.ml:127-138,
  *                                                src/PhyloCSFModel.ml:67-82
  *   - outside pass and branch posteriors ....... lib/CamlPaml/PhyloLik.ml:96-120,140-174
+ *   - sufficient statistics and ELL ............ lib/CamlPaml/PhyloEM.ml:14-20,22-73
  *   - dP/dt in the eigenbasis .................. lib/CamlPaml/Q.ml:260-275
  *   - find_init ................................ lib/CamlPaml/Fit.ml:27-48
  *   - bounded Brent maximiser .................. lib/CamlPaml/Fit.ml:3-24 (GSL "brent"
@@ -427,6 +428,94 @@ int orc_grad_branches(const orc_model *m, const orc_tree *tr, double rho, int nc
     free(dP);
     free((void *)Ps);
     *lpr_out = lpr;
+    return ORC_OK;
+}
+
+/* Expected substitution counts of every branch summed over the columns of a
+ * region: add_branch_posteriors (PhyloLik.ml:140-174) per column and branch, as
+ * PhyloEM.collect_sufficient_statistics accumulates them (PhyloEM.ml:14-20):
+ *   counts[i][a][b] += beta_p[a] (P_s alpha_s)[a] P_i[a][b] alpha_i[b] / z
+ * (rows with beta_p[a] = 0 skipped, columns with z = 0 add nothing).
+ * counts: [n-1][k][k], zeroed here.  lpr_out: sum of log z. */
+int orc_branch_counts(const orc_model *m, const orc_tree *tr, double rho, int ncols, const int *leaves,
+                      double *lpr_out, double *counts)
+{
+    int k = m->k, n = tr->n, nl = tr->nl;
+    double *Pflat = (double *)malloc(sizeof(double) * (size_t)(n - 1) * k * k);
+    const double **Ps = (const double **)malloc(sizeof(double *) * (n - 1));
+    int st = ORC_OK;
+    for (int i = 0; i < n - 1 && st == ORC_OK; i++) {
+        Ps[i] = Pflat + (size_t)i * k * k;
+        st = orc_pt(m, rho * tr->branch[i], Pflat + (size_t)i * k * k);
+    }
+    if (st != ORC_OK) { free(Pflat); free((void *)Ps); return st; }
+    double *alpha = (double *)malloc(sizeof(double) * (size_t)n * k);
+    double *beta = (double *)malloc(sizeof(double) * (size_t)n * k);
+    double *inter = (double *)malloc(sizeof(double) * k);
+    memset(counts, 0, sizeof(double) * (size_t)(n - 1) * k * k);
+    double lpr = 0.0;
+    for (int c = 0; c < ncols; c++) {
+        const int *lv = leaves + (size_t)c * nl;
+        double z = column_inside(k, tr, Ps, m->prior, lv, alpha, NULL);
+        lpr += log(z);
+        if (!(z > 0.0)) continue;
+        for (int a = 0; a < k; a++) beta[(size_t)(n - 1) * k + a] = m->prior[a];
+        for (int i = n - 2; i >= 0; i--) {
+            int p = tr->parent[i];
+            int s = (tr->lchild[p] == i) ? tr->rchild[p] : tr->lchild[p];
+            const double *ps = Ps[s], *pi_ = Ps[i];
+            for (int a = 0; a < k; a++) {
+                double d = 0.0;
+                for (int b = 0; b < k; b++) d += ps[a * k + b] * alpha[(size_t)s * k + b];
+                inter[a] = beta[(size_t)p * k + a] * d;
+            }
+            for (int b = 0; b < k; b++) {
+                double acc = 0.0;
+                for (int a = 0; a < k; a++) acc += inter[a] * pi_[a * k + b];
+                beta[(size_t)i * k + b] = acc;
+            }
+            double *ci = counts + (size_t)i * k * k;
+            for (int a = 0; a < k; a++) {
+                if (!(inter[a] > 0.0)) continue;
+                for (int b = 0; b < k; b++) ci[a * k + b] += inter[a] * pi_[a * k + b] * alpha[(size_t)i * k + b] / z;
+            }
+        }
+    }
+    free(alpha);
+    free(beta);
+    free(inter);
+    free(Pflat);
+    free((void *)Ps);
+    *lpr_out = lpr;
+    return ORC_OK;
+}
+
+/* Expected log-likelihood of sufficient statistics (PhyloEM.ell, PhyloEM.ml:22-73):
+ * branches_ell = sum_i sum_{ab: counts > 0} counts[i][a][b] log P_i[a][b] at t_i = rho b_i,
+ * prior_ell = sum_a (sum_b counts[lc][a][b]) log prior[a] (lc = the root's left child,
+ * terms with a positive row sum). */
+int orc_ell(const orc_model *m, const orc_tree *tr, double rho, const double *counts, double *ell_out)
+{
+    int k = m->k, n = tr->n;
+    double *P = (double *)malloc(sizeof(double) * (size_t)k * k);
+    double tot = 0.0;
+    int st = ORC_OK;
+    for (int i = 0; i < n - 1 && st == ORC_OK; i++) {
+        st = orc_pt(m, rho * tr->branch[i], P);
+        const double *ci = counts + (size_t)i * k * k;
+        for (int a = 0; a < k && st == ORC_OK; a++)
+            for (int b = 0; b < k; b++)
+                if (ci[a * k + b] > 0.0) tot += ci[a * k + b] * log(P[a * k + b]);
+    }
+    free(P);
+    if (st != ORC_OK) return st;
+    const double *cl = counts + (size_t)tr->lchild[n - 1] * k * k;
+    for (int a = 0; a < k; a++) {
+        double r = 0.0;
+        for (int b = 0; b < k; b++) r += cl[a * k + b];
+        if (r > 0.0) tot += r * log(m->prior[a]);
+    }
+    *ell_out = tot;
     return ORC_OK;
 }
 

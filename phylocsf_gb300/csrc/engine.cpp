@@ -1495,6 +1495,159 @@ static int score_impl(pcsf_engine *e, pcsf_batch *b, int strategy, pcsf_result *
 }
 
 // ---------------------------------------------------------------------------
+// Outside-pass products: expected branch counts and node posteriors
+// (PhyloLik.ml:96-174, PhyloEM.ml:14-20), one FP64 or FP32 P set per region.
+
+static int outside_impl(pcsf_engine *e, pcsf_batch *b, int model, const double *rho, double *counts, int n_sel,
+                        const int32_t *nodes, double *post, double *lpr, int32_t *status)
+{
+    const int nreg = b->nreg;
+    const bool fp64 = e->prec == PCSF_PREC_FP64;
+    const size_t es = fp64 ? 8 : 4;
+    const int comp = e->accurate_comp();
+    const int TC = outside_tile_cols();
+    std::vector<int32_t> sel;
+    if (n_sel > 0) {
+        sel.assign(e->n, -1);
+        for (int k = 0; k < n_sel; k++) {
+            if (nodes[k] < 0 || nodes[k] >= e->n) return e->fail(PCSF_EINVAL, "node %d is not in the tree", nodes[k]);
+            sel[nodes[k]] = k;   // a node listed twice is written to its last row
+        }
+    }
+    const size_t smem = outside_smem_bytes(fp64, e->nslots, e->nl, (int)e->sched.size());
+    if (smem > e->smem_optin) return e->fail(PCSF_EINVAL, "this tree needs %zu B of shared memory for the outside pass", smem);
+    const size_t scr = outside_scratch_per_cta(fp64, e->nl);
+    const size_t pset_bytes = (size_t)e->nbr * K2 * es;
+    const size_t cnt_bytes = counts ? (size_t)e->nbr * K2 * sizeof(double) : 0;
+    // regions per launch: P sets and counts of a chunk within ~2 GiB
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)std::max(nreg, 1),
+                                                                (size_t(2) << 30) / (pset_bytes + cnt_bytes)));
+    const int grid = std::max(1, std::min(e->sm_count, chunk));
+    DevBuf<unsigned char> dP, dscr;
+    DevBuf<double> dcnt, dlpr, dpost;
+    DevBuf<PSet> dps;
+    DevBuf<Request> dreq;
+    DevBuf<WorkItem> dwi;
+    DevBuf<int32_t> dwib, dstatus, dsel;
+    CK(dP.reserve((size_t)chunk * pset_bytes), "cudaMalloc P(t)");
+    CK(dscr.reserve((size_t)grid * scr), "cudaMalloc outside-pass scratch");
+    if (counts) CK(dcnt.reserve((size_t)chunk * e->nbr * K2), "cudaMalloc counts");
+    CK(dlpr.reserve(chunk), "cudaMalloc");
+    CK(dps.reserve(chunk), "cudaMalloc");
+    CK(dreq.reserve(chunk), "cudaMalloc");
+    CK(dwib.reserve(chunk + 1), "cudaMalloc");
+    CK(dstatus.reserve(chunk), "cudaMalloc");
+    cudaStream_t s = e->stream;
+    if (n_sel > 0) {
+        CK(dsel.reserve(e->n), "cudaMalloc");
+        CK(dpost.reserve((size_t)n_sel * std::max<int64_t>(b->total_cols, 1) * K), "cudaMalloc posteriors");
+        CK(cudaMemcpyAsync(dsel.p, sel.data(), sizeof(int32_t) * e->n, cudaMemcpyHostToDevice, s), "H2D");
+    }
+    for (int r0 = 0; r0 < nreg; r0 += chunk) {
+        const int r1 = std::min(nreg, r0 + chunk), nr = r1 - r0;
+        std::vector<PSet> ps(nr);
+        std::vector<Request> rq(nr);
+        std::vector<WorkItem> wis;
+        std::vector<int32_t> wib(nr + 1);
+        for (int r = 0; r < nr; r++) {
+            const int reg = r0 + r;
+            if (!(rho[reg] > 0.0) || !std::isfinite(rho[reg])) return e->fail(PCSF_EINVAL, "rho[%d] = %g", reg, rho[reg]);
+            ps[r] = PSet{model, 0, rho[reg]};
+            rq[r] = Request{reg, model, r, (uint32_t)b->offs[reg], rho[reg]};
+            wib[r] = (int)wis.size();
+            for (int64_t c = b->offs[reg]; c < b->offs[reg + 1]; c += TC)
+                wis.push_back(WorkItem{r, (int32_t)std::min<int64_t>(TC, b->offs[reg + 1] - c), c});
+        }
+        wib[nr] = (int)wis.size();
+        CK(dwi.reserve(std::max<size_t>(wis.size(), 1)), "cudaMalloc");
+        CK(cudaMemcpyAsync(dps.p, ps.data(), sizeof(PSet) * nr, cudaMemcpyHostToDevice, s), "H2D");
+        CK(cudaMemcpyAsync(dreq.p, rq.data(), sizeof(Request) * nr, cudaMemcpyHostToDevice, s), "H2D");
+        if (!wis.empty()) CK(cudaMemcpyAsync(dwi.p, wis.data(), sizeof(WorkItem) * wis.size(), cudaMemcpyHostToDevice, s), "H2D");
+        CK(cudaMemcpyAsync(dwib.p, wib.data(), sizeof(int32_t) * (nr + 1), cudaMemcpyHostToDevice, s), "H2D");
+        CK(cudaMemsetAsync(dstatus.p, 0x7f, sizeof(int32_t) * nr, s), "memset");
+        if (counts) CK(cudaMemsetAsync(dcnt.p, 0, sizeof(double) * (size_t)nr * e->nbr * K2, s), "memset");
+        CK(launch_pform(fp64, dps.p, nr, e->dbranch.p, e->nbr, e->dm, dP.p, dstatus.p, s), "P(t) formation launch");
+        OutsideArgs oa{};
+        oa.wi = dwi.p;
+        oa.wi_begin = dwib.p;
+        oa.nreq = nr;
+        oa.req = dreq.p;
+        oa.leaves = b->dleaves.p;
+        oa.Pbuf = dP.p;
+        oa.sched = e->dsched.p;
+        oa.n_internal = (int)e->sched.size();
+        oa.nl = e->nl;
+        oa.nbr = e->nbr;
+        oa.nslots = e->nslots;
+        oa.m = e->dm;
+        oa.scratch = dscr.p;
+        oa.scratch_per_cta = scr;
+        oa.lpr = dlpr.p;
+        oa.counts = counts ? dcnt.p : nullptr;
+        oa.sel = n_sel > 0 ? dsel.p : nullptr;
+        oa.post = dpost.p;
+        oa.total_cols = b->total_cols;
+        CK(launch_outside(fp64, comp, oa, s, std::min(grid, nr)), "outside-pass launch");
+        e->stats.kernel_launches += 2;
+        std::vector<int32_t> keys(nr);
+        std::vector<double> hl(nr);
+        CK(cudaMemcpyAsync(keys.data(), dstatus.p, sizeof(int32_t) * nr, cudaMemcpyDeviceToHost, s), "D2H");
+        CK(cudaMemcpyAsync(hl.data(), dlpr.p, sizeof(double) * nr, cudaMemcpyDeviceToHost, s), "D2H");
+        if (counts)
+            CK(cudaMemcpyAsync(counts + (size_t)r0 * e->nbr * K2, dcnt.p, sizeof(double) * (size_t)nr * e->nbr * K2,
+                               cudaMemcpyDeviceToHost, s), "D2H counts");
+        CK(cudaStreamSynchronize(s), "outside pass");
+        for (int r = 0; r < nr; r++) {
+            if (lpr) lpr[r0 + r] = hl[r];
+            if (status) status[r0 + r] = (keys[r] >= 0 && keys[r] < 0x7f000000) ? (keys[r] & 15) : PCSF_OK;
+        }
+    }
+    if (n_sel > 0 && b->total_cols > 0)
+        CK(cudaMemcpy(post, dpost.p, sizeof(double) * (size_t)n_sel * b->total_cols * K, cudaMemcpyDeviceToHost),
+           "D2H posteriors");
+    return PCSF_OK;
+}
+
+// PhyloEM.ell (PhyloEM.ml:22-73) of counts [nbr][K][K] at tree scale rho: the branches'
+// sum of counts x log P (positive counts only) with P(t) formed in FP64, plus the root
+// prior term from the row sums of the root's left child's counts.
+static int ell_impl(pcsf_engine *e, int model, double rho, const double *counts, double *ell)
+{
+    DevBuf<double> dP;
+    DevBuf<PSet> dps;
+    DevBuf<int32_t> dst;
+    CK(dP.reserve((size_t)e->nbr * K2), "cudaMalloc");
+    CK(dps.reserve(1), "cudaMalloc");
+    CK(dst.reserve(1), "cudaMalloc");
+    PSet ps{model, 0, rho};
+    CK(cudaMemcpyAsync(dps.p, &ps, sizeof ps, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemsetAsync(dst.p, 0x7f, sizeof(int32_t), e->stream), "memset");
+    CK(launch_pform(true, dps.p, 1, e->dbranch.p, e->nbr, e->dm, dP.p, dst.p, e->stream), "P(t) launch");
+    e->stats.kernel_launches += 1;
+    std::vector<double> Et((size_t)e->nbr * K2);
+    int32_t key = STATUS_NONE;
+    CK(cudaMemcpyAsync(Et.data(), dP.p, sizeof(double) * Et.size(), cudaMemcpyDeviceToHost, e->stream), "D2H");
+    CK(cudaMemcpyAsync(&key, dst.p, sizeof(int32_t), cudaMemcpyDeviceToHost, e->stream), "D2H");
+    CK(cudaStreamSynchronize(e->stream), "P(t)");
+    if (key >= 0 && key < 0x7f000000) return e->fail(key & 15, "P(t) formation failed at tree scale %g", rho);
+    double tot = 0.0;
+    for (int i = 0; i < e->nbr; i++)
+        for (int a = 0; a < K; a++)
+            for (int c = 0; c < K; c++) {
+                const double x = counts[((size_t)i * K + a) * K + c];
+                if (x > 0.0) tot += x * std::log(Et[(size_t)i * K2 + (size_t)c * K + a] + (a == c ? 1.0 : 0.0));
+            }
+    const double *cl = counts + (size_t)e->lch[e->n - 1] * K2;
+    for (int a = 0; a < K; a++) {
+        double r = 0.0;
+        for (int c = 0; c < K; c++) r += cl[a * K + c];
+        if (r > 0.0) tot += r * std::log(e->prior[model][a]);
+    }
+    *ell = tot;
+    return PCSF_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Read-only view of an engine's device state for pcsf_lpr_noalloc (noalloc.cu).
 
 int pcsf_internal_noalloc_ctx(pcsf_engine *e, NoallocCtx *c)
@@ -2361,6 +2514,42 @@ int pcsf_lpr(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, do
         if (status) status[r] = res[r].status;
     }
     return PCSF_OK;
+}
+
+int pcsf_branch_counts(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, double *counts, double *lpr,
+                       int32_t *status)
+{
+    if (!e) return PCSF_EINVAL;
+    if (!e->has_models) return e->fail(PCSF_EINVAL, "this engine has no coding / noncoding models");
+    CK(cudaSetDevice(e->device), "cudaSetDevice");
+    if (!b || b->e != e) return e->fail(PCSF_EINVAL, "pcsf_branch_counts: batch does not belong to this engine");
+    if (model < 0 || model > 1) return e->fail(PCSF_EINVAL, "pcsf_branch_counts: model %d", model);
+    if (b->nreg > 0 && (!rho || !counts)) return e->fail(PCSF_EINVAL, "pcsf_branch_counts: null argument");
+    return outside_impl(e, b, model, rho, counts, 0, nullptr, nullptr, lpr, status);
+}
+
+int pcsf_node_posteriors(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, int32_t n_nodes,
+                         const int32_t *nodes, double *post, int32_t *status)
+{
+    if (!e) return PCSF_EINVAL;
+    if (!e->has_models) return e->fail(PCSF_EINVAL, "this engine has no coding / noncoding models");
+    CK(cudaSetDevice(e->device), "cudaSetDevice");
+    if (!b || b->e != e) return e->fail(PCSF_EINVAL, "pcsf_node_posteriors: batch does not belong to this engine");
+    if (model < 0 || model > 1) return e->fail(PCSF_EINVAL, "pcsf_node_posteriors: model %d", model);
+    if (n_nodes < 0 || (n_nodes > 0 && (!nodes || !post)) || (b->nreg > 0 && !rho))
+        return e->fail(PCSF_EINVAL, "pcsf_node_posteriors: null argument");
+    if (n_nodes == 0) return PCSF_OK;
+    return outside_impl(e, b, model, rho, nullptr, n_nodes, nodes, post, nullptr, status);
+}
+
+int pcsf_ell(pcsf_engine *e, int32_t model, double rho, const double *counts, double *ell)
+{
+    if (!e) return PCSF_EINVAL;
+    if (!e->has_models) return e->fail(PCSF_EINVAL, "this engine has no coding / noncoding models");
+    CK(cudaSetDevice(e->device), "cudaSetDevice");
+    if (model < 0 || model > 1 || !counts || !ell) return e->fail(PCSF_EINVAL, "pcsf_ell: bad argument");
+    if (!(rho > 0.0) || !std::isfinite(rho)) return e->fail(PCSF_EINVAL, "pcsf_ell: rho = %g", rho);
+    return ell_impl(e, model, rho, counts, ell);
 }
 
 int pcsf_grad(pcsf_engine *e, pcsf_batch *b, int32_t model, const double *rho, double *lpr, double *d_branch,

@@ -190,6 +190,32 @@ int ff_tile_cols();
 size_t prune_ff_smem_bytes(int nslots, int nl, int nint);
 int prune_ff_ctas_per_sm(int nslots, int nl, int nint);
 
+// Outside-pass products (outside_kernels.cu): per request (one CTA at a time, tiles of
+// outside_tile_cols() columns in order) the log-likelihood, optionally the expected
+// substitution counts of every branch and the posteriors of selected nodes.
+struct OutsideArgs {
+    const WorkItem *wi;          // work items, contiguous per request
+    const int32_t *wi_begin;     // [nreq + 1]
+    int nreq;
+    const Request *req;          // Request.pset indexes Pbuf
+    const uint8_t *leaves;       // [total_cols][nl]
+    const void *Pbuf;            // per P set [nbr][K][K] E^T, FP64 or FP32
+    const SchedNode *sched;
+    int n_internal, nl, nbr, nslots;
+    DevModels m;
+    void *scratch;               // gridDim.x * scratch_per_cta bytes
+    size_t scratch_per_cta;
+    double *lpr;                 // [nreq]
+    double *counts;              // [nreq][nbr][K][K], zeroed by the caller; null: none
+    const int32_t *sel;          // [n] output row of each node, -1 if not selected; null: no posteriors
+    double *post;                // [n_selected][total_cols][K]
+    int64_t total_cols;
+};
+cudaError_t launch_outside(bool fp64, int comp, const OutsideArgs &a, cudaStream_t s, int grid);
+int outside_tile_cols();
+size_t outside_smem_bytes(bool fp64, int nslots, int nl, int nint);
+size_t outside_scratch_per_cta(bool fp64, int nl);
+
 // Read-only view of an engine's device state for the allocation-free entry point
 // (noalloc.cu; filled by engine.cpp).
 struct NoallocCtx {

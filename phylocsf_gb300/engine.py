@@ -119,6 +119,9 @@ SIGNATURES = {
                            _U8], ctypes.c_int),
     "pcsf_engine_set_exact_threshold": ([_VP, ctypes.c_int64], ctypes.c_int),
     "pcsf_engine_exact_available": ([_VP], ctypes.c_int),
+    "pcsf_branch_counts": ([_VP, _VP, ctypes.c_int32, _D, _D, _D, _I32], ctypes.c_int),
+    "pcsf_ell": ([_VP, ctypes.c_int32, ctypes.c_double, _D, _D], ctypes.c_int),
+    "pcsf_node_posteriors": ([_VP, _VP, ctypes.c_int32, _D, ctypes.c_int32, _I32, _D, _I32], ctypes.c_int),
     "pcsf_lpr_noalloc": ([_VP, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, _I64, ctypes.c_void_p, ctypes.c_void_p,
                           ctypes.c_void_p], ctypes.c_int),
     "pcsf_simulate": ([ctypes.c_int32, _I32, ctypes.c_int32, _D, _D, ctypes.c_int32, _I64, _I32, _D, ctypes.c_int32,
@@ -425,6 +428,40 @@ class Engine:
                                   _p(db, ctypes.c_double) if branches else None, _p(drho, ctypes.c_double),
                                   _p(st, ctypes.c_int32)), self.handle)
         return lpr, db, drho, st
+
+    # ---- outside-pass statistics (PhyloEM sufficient statistics, node posteriors)
+    def branch_counts(self, batch: Batch, model: int, rho):
+        """(counts [n_regions][n-1][64][64], lpr, status): expected substitution counts of every
+        branch summed over each region's columns (PhyloEM.collect_sufficient_statistics)."""
+        r = np.ascontiguousarray(np.broadcast_to(np.asarray(rho, np.float64), (batch.n_regions,)))
+        nbr = self.tree.n - 1
+        counts = np.zeros((batch.n_regions, nbr, 64, 64))
+        lpr = np.zeros(batch.n_regions)
+        st = np.zeros(batch.n_regions, np.int32)
+        _check(self.lib.pcsf_branch_counts(self.handle, batch.handle, model, _p(r, ctypes.c_double),
+                                           _p(counts, ctypes.c_double), _p(lpr, ctypes.c_double),
+                                           _p(st, ctypes.c_int32)), self.handle)
+        return counts, lpr, st
+
+    def ell(self, model: int, rho: float, counts) -> float:
+        """PhyloEM.ell of one set of sufficient statistics [n-1][64][64] at tree scale rho."""
+        c = np.ascontiguousarray(counts, np.float64)
+        out = ctypes.c_double()
+        _check(self.lib.pcsf_ell(self.handle, model, float(rho), _p(c, ctypes.c_double), ctypes.byref(out)),
+               self.handle)
+        return out.value
+
+    def node_posteriors(self, batch: Batch, model: int, rho, nodes):
+        """(post [len(nodes)][total_cols][64], status): PhyloLik.node_posterior of the given nodes at
+        every column of the batch."""
+        r = np.ascontiguousarray(np.broadcast_to(np.asarray(rho, np.float64), (batch.n_regions,)))
+        nd = np.ascontiguousarray(nodes, np.int32)
+        post = np.zeros((len(nd), batch.total_cols, 64))
+        st = np.zeros(batch.n_regions, np.int32)
+        _check(self.lib.pcsf_node_posteriors(self.handle, batch.handle, model, _p(r, ctypes.c_double), len(nd),
+                                             _p(nd, ctypes.c_int32), _p(post, ctypes.c_double),
+                                             _p(st, ctypes.c_int32)), self.handle)
+        return post, st
 
     # ---- model introspection
     def pt(self, model: int, t) -> Tuple[np.ndarray, np.ndarray]:

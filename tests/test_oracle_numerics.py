@@ -84,3 +84,24 @@ def test_empty_region_mle():
     mc, mn, ot, tree = H.oracle_models("12flies")
     r = O.score_region(mc, mn, ot, O.MLE, np.zeros((0, tree.nl), np.int32))
     assert r.status == 0 and r.score == 0.0 and r.rho_c == 10.0 and r.rho_n == 10.0
+
+
+def test_oracle_branch_counts_identities():
+    """The oracle's sufficient statistics (PhyloEM.ml:14-20): every branch's expected counts sum to
+    the number of columns, the counts' ELL is at most lpr (Gibbs: ELL - lpr = -entropy of the
+    hidden states <= 0), and at fixed counts d ELL / d rho = d lpr / d rho (Fisher identity)."""
+    from phylocsf_gb300 import synth
+    mc, mn, ot, tree = H.oracle_models("12flies")
+    ps = synth.load_params("12flies")
+    offs, lv = synth.simulate(ps, np.array([60]), np.array([0], np.int32), np.full((1, 12), 0.2), 3)
+    x = H.u8_to_oracle(lv)
+    rho = 0.8
+    lpr, c = O.branch_counts(mc, ot, rho, x)
+    assert lpr == pytest.approx(O.lpr_leaves(mc, ot, rho, x)[0], rel=1e-12)
+    np.testing.assert_allclose(c.sum(axis=(1, 2)), 60.0, rtol=1e-12)
+    assert (c >= 0).all()
+    assert O.ell(mc, ot, rho, c) <= lpr
+    h = 1e-6
+    dell = (O.ell(mc, ot, rho + h, c) - O.ell(mc, ot, rho - h, c)) / (2 * h)
+    dlpr = (O.lpr_leaves(mc, ot, rho + h, x)[0] - O.lpr_leaves(mc, ot, rho - h, x)[0]) / (2 * h)
+    assert dell == pytest.approx(dlpr, rel=1e-6)
