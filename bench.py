@@ -47,7 +47,8 @@ DATA = "synthetic (seeded simulation along the tree; no public benchmark exists)
 L2_BYTES = 129 * 1024 * 1024
 DTYPES = {"fp32": "f32", "fp32c": "f32 (compensated)", "fp32b": "f32 (blocked compensation)", "fp64": "f64",
           "tf32x3": "tf32x3 search, f32 (compensated) reported",
-          "tf32x3b": "tf32x3 search, f32 (blocked compensation) reported"}
+          "tf32x3b": "tf32x3 search, f32 (blocked compensation) reported",
+          "bf16x3b": "3xbf16 split search, f32 (blocked compensation) reported"}
 
 
 def flops_per_column(nl: int) -> int:
@@ -68,7 +69,7 @@ def flops_per_column_tangent(nl: int) -> int:
     return 8192 * (3 * (nl - 2) + nl) + 64 * 4 * (nl - 1) + 256
 
 
-KERNEL_NAMES = {0: "k_prune (SIMT, {prec} returned values)", 1: "k_prune_tc<3> (tcgen05 search)",
+KERNEL_NAMES = {0: "k_prune (SIMT, {prec} returned values)", 1: "{tc} (tcgen05 search)",
                 2: "k_grad (adjoint)", 3: "k_prune_tc_dual (tcgen05 tangent)",
                 4: "k_prune_ff (float-float returned values of long regions)"}
 KERNEL_KEYS = {0: "simt_prune", 1: "tc_prune", 2: "grad", 3: "tc_tangent", 4: "ff_prune"}
@@ -414,7 +415,9 @@ def run_ours(args, world, rank, local):
     # requires, with the FP32 FMA ceiling alongside.
     peaks, peak_kind = load_peaks()
     kind = int(np.argmax(st["kind_ms"]))
-    kname = KERNEL_NAMES[kind].format(prec=args.precision)
+    kname = KERNEL_NAMES[kind].format(prec=args.precision,
+                                      tc="k_prune_bf16 (6 BF16 products)" if args.precision.startswith("bf16")
+                                      else "k_prune_tc<3>")
     kcols = st["kind_columns"][kind]
     kflops = kcols * {0: flops_per_column, 1: flops_per_column, 2: flops_per_column_grad,
                       3: flops_per_column_tangent, 4: flops_per_column}[kind](nl)

@@ -51,7 +51,8 @@ extern "C" {
 #define PCSF_PREC_FP64 0  /* FP64 everywhere: the oracle-matched plain GPU path      */
 #define PCSF_PREC_FP32 1  /* FP32 contractions on P(t)-I, FP64 eigensystem and sums  */
 #define PCSF_PREC_TF32X3 2 /* tcgen05 TF32 hi/lo split (3 products), FP32 accumulate */
-#define PCSF_PREC_BF16X3 3 /* reserved, not built: engine creation fails with PCSF_EINVAL (BF16 keeps 8 bits, so a 3-product split stops near 16; TF32x3 reaches ~22) */
+#define PCSF_PREC_BF16X3 3 /* tcgen05 BF16 split x = h + m + l (exact), the 6 products
+                              that reach FP32 accuracy, FP32 accumulate                 */
 #define PCSF_PREC_TF32 4  /* tcgen05 single TF32 product (precision study only)      */
 
 /* engine flag: compensated (Kahan) summation in the FP32 contractions.  FP32

@@ -19,7 +19,7 @@ BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libphylocsf_gb300.so")
 
-SOURCES = ["kernels.cu", "grad_kernels.cu", "tc_kernels.cu", "tc_pform.cu", "tc_dual.cu", "noalloc.cu", "ff_kernels.cu", "outside_kernels.cu", "engine.cpp", "host_io.cpp"]
+SOURCES = ["kernels.cu", "grad_kernels.cu", "tc_kernels.cu", "tc_pform.cu", "tc_dual.cu", "tc_bf16.cu", "noalloc.cu", "ff_kernels.cu", "outside_kernels.cu", "engine.cpp", "host_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include")]
 

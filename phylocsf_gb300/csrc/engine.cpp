@@ -196,6 +196,12 @@ struct pcsf_engine {
     }
 };
 
+// precisions whose search evaluations run on the tensor cores
+static inline bool tc_prec(int prec)
+{
+    return prec == PCSF_PREC_TF32X3 || prec == PCSF_PREC_TF32 || prec == PCSF_PREC_BF16X3;
+}
+
 struct pcsf_batch {
     pcsf_engine *e = nullptr;
     int nreg = 0;
@@ -541,7 +547,8 @@ static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2],
 static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t flags)
 {
     int prec = flags & 0xff;
-    if (prec != PCSF_PREC_FP64 && prec != PCSF_PREC_FP32 && prec != PCSF_PREC_TF32X3 && prec != PCSF_PREC_TF32)
+    if (prec != PCSF_PREC_FP64 && prec != PCSF_PREC_FP32 && prec != PCSF_PREC_TF32X3 && prec != PCSF_PREC_TF32 &&
+        prec != PCSF_PREC_BF16X3)
         return e->fail(PCSF_EINVAL, "precision mode %d is not available in this build", prec);
     e->prec = prec;
     e->compensated = (flags & PCSF_COMPENSATED) != 0;
@@ -575,6 +582,14 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
     CK(e->derr.reserve(1), "cudaMalloc");
     CK(cudaMemsetAsync(e->derr.p, 0, sizeof(int), e->stream), "memset");
     const bool tc = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
+    if (e->prec == PCSF_PREC_BF16X3) {
+        if (!prune_bf16_supported(e->nslots, e->nl))
+            return e->fail(PCSF_EINVAL, "BF16 tensor-core path supports up to 160 leaves and 8 partial slots");
+        if (prune_bf16_smem_bytes(e->nl, (int)e->sched.size()) > (size_t)prop.sharedMemPerBlockOptin)
+            return e->fail(PCSF_EINVAL, "BF16 tensor-core path needs %zu B shared memory",
+                           prune_bf16_smem_bytes(e->nl, (int)e->sched.size()));
+        e->tc_grid = prop.multiProcessorCount * prune_bf16_ctas_per_sm(e->nslots, e->nl, (int)e->sched.size());
+    }
     if (tc && !prune_tc_supported(e->nslots, e->nl))
         return e->fail(PCSF_EINVAL, "tensor-core path supports up to 160 leaves and 8 partial slots (tree: %d, %d)",
                        e->nl, e->nslots);
@@ -649,11 +664,11 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     const DevModels dmv = dyn ? *dyn : e->dm;
     if (drho && (grad || dyn || accurate || !e->dual_ok))
         return e->fail(PCSF_EINVAL, "d lpr / d rho by the tangent pass needs a tensor-core engine and a tree of <= 4 slots");
-    const bool tc = (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32) && !accurate;
+    const bool tc = tc_prec(e->prec) && !accurate;
     // the gradient always runs the SIMT adjoint kernel (64-column tiles in FP32)
     const int TC = grad ? (e->prec == PCSF_PREC_FP64 ? 32 : 64)
                         : ff ? ff_tile_cols() : !tc ? simt_tile_cols(e->prec, e->nslots) : prune_tile_cols(e->prec);
-    const int comp = (accurate && (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32)) ? e->accurate_comp()
+    const int comp = (accurate && tc_prec(e->prec)) ? e->accurate_comp()
                                                                                               : e->comp_mode();
 
     const int kind = drho ? 3 : grad ? 2 : tc ? 1 : ff ? 4 : 0;
@@ -751,7 +766,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     const bool stage64 = (dyn || e->pt64) && e->prec != PCSF_PREC_FP64 && !ff;   // FP64 formation, then FP32 storage
     if (stage64 || ff) CK(e->Pbuf64.reserve(max_chunk_ps * (size_t)e->nbr * K2), "cudaMalloc P(t) staging buffer");
     const int nbop = e->nbr - e->nl;
-    const bool want_bop = tc && !grad;
+    const bool want_bop = tc && !grad && e->prec != PCSF_PREC_BF16X3;   // the BF16 kernel splits E^T itself
     if (want_bop) CK(e->Bop.reserve(max_chunk_ps * (size_t)nbop * 2 * K2), "cudaMalloc tensor-core operand buffer");
     float *bop = want_bop ? e->Bop.p : nullptr;
     size_t gscr = 0;
@@ -849,7 +864,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
             ga.partials = pa.partials;
             ga.gpart = e->dgpart.p + (size_t)wib[r0] * gstride;
             int grid = std::min(e->grad_grid, std::max(pa.nwi, 1));
-            const bool tce = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
+            const bool tce = tc_prec(e->prec);
             CK(launch_grad(e->prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32,
                            tce ? e->accurate_comp() : e->comp_mode(), ga, s, grid), "gradient launch");
         } else if (drho) {
@@ -861,7 +876,10 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
             CK(launch_prune_ff(pa, s, grid), "float-float pruning launch");
         } else if (tc) {
             int grid = std::min(e->tc_grid, std::max(pa.nwi, 1));
-            CK(launch_prune_tc(e->prec == PCSF_PREC_TF32X3 ? 3 : 1, pa, e->derr.p, s, grid), "tensor-core pruning launch");
+            if (e->prec == PCSF_PREC_BF16X3)
+                CK(launch_prune_bf16(pa, e->derr.p, s, grid), "BF16 tensor-core pruning launch");
+            else
+                CK(launch_prune_tc(e->prec == PCSF_PREC_TF32X3 ? 3 : 1, pa, e->derr.p, s, grid), "tensor-core pruning launch");
         } else {
             int grid = std::min(e->prune_grid, std::max(pa.nwi, 1));
             CK(launch_prune(e->prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32, comp, pa, s, grid),
@@ -1464,7 +1482,7 @@ static int score_impl(pcsf_engine *e, pcsf_batch *b, int strategy, pcsf_result *
             f.model = m;
             f.ncols = b->offs[r + 1] - b->offs[r];
             f.deriv = e->prec != PCSF_PREC_FP64;
-            f.tc_search = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
+            f.tc_search = tc_prec(e->prec);
             f.exact = is_exact(e, f.ncols);
             f.accurate_final = f.tc_search || f.exact;
             if (strategy == PCSF_FIXED) {
@@ -1657,7 +1675,7 @@ int pcsf_internal_noalloc_ctx(pcsf_engine *e, NoallocCtx *c)
     c->device = e->device;
     c->stream = e->stream;
     c->prec = e->prec;
-    const bool tcprec = e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32;
+    const bool tcprec = tc_prec(e->prec);
     // pcsf_lpr's returned values: the SIMT kernel with the accurate summation on
     // tensor-core engines, the engine's own summation otherwise
     c->comp = tcprec ? e->accurate_comp() : e->comp_mode();

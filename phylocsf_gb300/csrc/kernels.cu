@@ -636,7 +636,7 @@ __global__ void __launch_bounds__(PR_THREADS) k_prune(PruneArgs a)
 
 int prune_tile_cols(int prec)
 {
-    if (prec == PCSF_PREC_TF32X3 || prec == PCSF_PREC_TF32) return 128;
+    if (prec == PCSF_PREC_TF32X3 || prec == PCSF_PREC_TF32 || prec == PCSF_PREC_BF16X3) return 128;
     return prec == PCSF_PREC_FP64 ? 32 : 64;
 }
 

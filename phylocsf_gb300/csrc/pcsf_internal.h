@@ -162,6 +162,12 @@ cudaError_t launch_prune_tc(int nprod, const PruneArgs &a, int *err, cudaStream_
 size_t prune_tc_smem_bytes(int nl, int nint);
 bool prune_tc_supported(int nslots, int nl);
 int prune_tc_ctas_per_sm(int nslots, int nl, int nint);
+// Tensor-core pruning with BF16 split products (tc_bf16.cu): x = h + m + l, six
+// products on tcgen05 kind::f16, FP32 accumulation; E^T of every branch in Pbuf (FP32).
+cudaError_t launch_prune_bf16(const PruneArgs &a, int *err, cudaStream_t s, int grid);
+size_t prune_bf16_smem_bytes(int nl, int nint);
+bool prune_bf16_supported(int nslots, int nl);
+int prune_bf16_ctas_per_sm(int nslots, int nl, int nint);
 // tensor-core P(t) formation for the search evaluations (tc_pform.cu): E^T of the
 // branches above leaves into Pbuf, B operands of the branches above internal
 // nodes into Bop; Bpf = per model the pre-split B = U^T D^1/2 [2][hi, lo][64 x 64]

@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(TD_THREADS, 1) k_prune_tc_dual(PruneArgs a, co
         }
         pf_next();                       // while the MMAs run
         const bool done = mbar_wait(barM, ph_mma);
-        ph_mma ^= 1u;
+        if (done) ph_mma ^= 1u;   // after a timed-out wait the quiesce waits for this phase
         tc_fence_after();
         return done;
     };

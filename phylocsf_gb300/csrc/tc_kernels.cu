@@ -367,9 +367,9 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
                     leaf_fix(ls0, v);
                 }
                 const bool done = mbar_wait(barM, ph_mma);
-                ph_mma ^= 1u;
                 tc_fence_after();
                 if (!done) bad = true;
+                else ph_mma ^= 1u;   // after a timed-out wait the quiesce waits for this phase
                 if (tid == 0 && done) issue_next_b();     // the B operand is free again
                 child_value(s, r, v, have);
                 have = true;

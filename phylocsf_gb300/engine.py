@@ -30,7 +30,9 @@ PREC = {"fp64": 0, "fp32": 1, "tf32x3": 2, "bf16x3": 3, "tf32": 4,
         "fp32c": 1 | (1 << 16),      # FP32 contractions with compensated summation
         "fp32b": 1 | (1 << 18),      # FP32 contractions with blocked compensation
         "tf32x3b": 2 | (1 << 18),    # tensor-core search, blocked-compensation returned values
+        "bf16x3b": 3 | (1 << 18),    # BF16-split tensor-core search, blocked-compensation returned values
         "tf32x3_direct": 2 | (1 << 17), "tf32_direct": 4 | (1 << 17),   # lpr straight from the tensor cores
+        "bf16x3_direct": 3 | (1 << 17),
         "fp32b_pt64": 1 | (1 << 18) | (1 << 19)}   # FP64-formed P(t) stored in FP32 (accuracy studies)
 MARGINALIZE = 64
 ORF_MODES = {"asis": 0, "atgstop": 1, "stopstop": 2, "stopstop3": 3, "tofirststop": 4,

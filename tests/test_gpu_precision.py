@@ -6,9 +6,11 @@ Per alignment: relative logL error of each model and |d score| of the fixed-stra
 score.  Bounds (the measured values are printed):
   - tensor cores, TF32 single product (tf32_direct): relative logL error <= 2e-3;
   - tensor cores, TF32 hi/lo x3 (tf32x3_direct): relative logL error <= 2e-6;
-  - returned values of the tensor-core engine (tf32x3b, compensated SIMT kernel) and the
-    compensated FP32 engines: |d score| <= 1e-3 dB for every alignment.
-A 3xBF16 split is not built (TF32x3 recovers the same ~22 bits with three products).
+  - tensor cores, 3xBF16 split x = h + m + l with the six products that reach FP32
+    accuracy (bf16x3_direct): relative logL error <= 2e-6;
+  - returned values of the tensor-core engines (tf32x3b, bf16x3b: compensated SIMT and
+    float-float kernels) and the compensated FP32 engines: |d score| <= 1e-3 dB for every
+    alignment.
 """
 import numpy as np
 import pytest
@@ -44,8 +46,9 @@ def _lprs(workload, prec):
 
 
 @pytest.mark.parametrize("prec,rel_bound,db_bound", [("tf32_direct", 2e-3, None), ("tf32x3_direct", 2e-6, None),
-                                                     ("tf32x3b", None, 1e-3), ("fp32b", None, 1e-3),
-                                                     ("fp32c", None, 1e-3)])
+                                                     ("bf16x3_direct", 2e-6, None),
+                                                     ("tf32x3b", None, 1e-3), ("bf16x3b", None, 1e-3),
+                                                     ("fp32b", None, 1e-3), ("fp32c", None, 1e-3)])
 def test_120mammals_precision(workload, reference, prec, rel_bound, db_bound):
     c64, n64 = reference
     c, n = _lprs(workload, prec)

@@ -93,7 +93,24 @@ def test_tf32_single_product_runs():
         assert abs(lpr[r] - lo) <= 1e-3 * abs(lo)
 
 
-@pytest.mark.parametrize("prec", ["tf32x3", "tf32x3b"])
+@pytest.mark.parametrize("name", ["12flies", "58mammals", "120mammals"])
+def test_bf16x3_lpr_matches_fp64(name):
+    """The 3xBF16 split-product kernel (tcgen05 kind::f16) against the FP64 engine: lpr within
+    2e-6 relative (measured ~4e-8, as the TF32x3 kernel), on tiles of 1, 127, 128, 129 and 700
+    columns."""
+    e = engine(name, "bf16x3_direct")
+    e64 = engine(name, "fp64")
+    offs, leaves = _data(name, [1, 127, 128, 129, 700], seed=3)
+    b, b64 = e.batch(offs, leaves), e64.batch(offs, leaves)
+    for model in (0, 1):
+        for rho in (0.3, 1.0, 4.0):
+            l, _, st = e.lpr(b, model, rho)
+            l64, _, _ = e64.lpr(b64, model, rho)
+            assert (st == 0).all()
+            assert np.all(np.abs(l - l64) <= 2e-6 * np.abs(l64)), (model, rho, l - l64)
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "tf32x3b", "bf16x3b"])
 def test_tf32x3_mle_close_to_fp64(prec):
     offs, leaves = _data("58mammals", list(np.random.default_rng(2).integers(50, 3000, size=64)), seed=2)
     a = engine("58mammals", "fp64").score_batch(offs, leaves, P.MLE)
@@ -130,11 +147,12 @@ def test_benchmark_workload_mle_within_contract(workload, n):
     assert d.max() <= 1e-3, np.sort(d)[-8:]
 
 
+@pytest.mark.parametrize("prec", ["tf32x3", "bf16x3b"])
 @pytest.mark.parametrize("idx", [0, 1, 2, 3])
-def test_tf32x3_reference_pins(idx):
+def test_tf32x3_reference_pins(idx, prec):
     p = H.pins()[idx]
     f = H.parse_flags(p["flags"])
-    e = engine(p["params"], "tf32x3")
+    e = engine(p["params"], prec)
     ex = H.examples()[p["file"]]
     mfa = "\n".join(">%s\n%s" % (s, r) for s, r in zip(ex["species"], ex["rows"])) + "\n"
     opts = D.Options(strategy=P.MLE, frames=f["frames"], orf_mode=f["orf"], remove_ref_gaps=f["remove_ref_gaps"],
