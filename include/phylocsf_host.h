@@ -56,6 +56,17 @@ int pcsf_pack_regions(int32_t n_leaves, const int32_t *leaf_rows, int32_t n_rows
                       const char *const *rows_rc, int64_t len, int32_t n_regions, const int32_t *rc,
                       const int64_t *lo, const int64_t *hi, int64_t *col_offsets, uint8_t *leaves);
 
+/* Per nucleotide column of an alignment, the total branch length of the smallest
+ * subtree spanning the species present in that column (not '-', '.' or 'N'),
+ * without the root branch: Newick.subtree + Newick.total_length
+ * (lib/CamlPaml/Newick.ml:34-61) as the branch length score takes them per column
+ * (src/PhyloCSF.ml:252-262).  A branch above node v belongs to it exactly when some
+ * but not all of the present species lie below v.  leaf_rows[l]: the row of tree
+ * leaf l or -1 when absent; rows: [n_rows] strings of length len; out: [len].
+ * The score of columns lo..hi is sum(out[lo..hi]) / (total tree length x (hi-lo+1)). */
+int pcsf_bls_columns(int32_t n_leaves, const int32_t *parent, const double *branch, const int32_t *leaf_rows,
+                     int32_t n_rows, const char *const *rows, int64_t len, double *out);
+
 /* Simulate codon columns along the tree (PhyloModel.simulate,
  * lib/CamlPaml/PhyloModel.ml:38-54: root ~ prior, each child ~ the P row of its
  * parent's state) for synthetic workloads.  P: [n_models][2*n_leaves-2][64][64]

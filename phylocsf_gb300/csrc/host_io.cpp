@@ -401,6 +401,35 @@ int pcsf_candidate_regions(const char *ref, int64_t len, int32_t frames, int32_t
     return PCSF_OK;
 }
 
+int pcsf_bls_columns(int32_t n_leaves, const int32_t *parent, const double *branch, const int32_t *leaf_rows,
+                     int32_t n_rows, const char *const *rows, int64_t len, double *out)
+{
+    if (n_leaves < 2 || !parent || !branch || !leaf_rows || (n_rows > 0 && !rows) || len < 0 || (len > 0 && !out))
+        return fail(PCSF_EINVAL, "pcsf_bls_columns: bad argument");
+    const int nl = n_leaves, n = 2 * nl - 1;
+    for (int i = 0; i < n - 1; i++)
+        if (parent[i] <= i || parent[i] >= n) return fail(PCSF_EINVAL, "pcsf_bls_columns: tree is not in T order");
+    for (int l = 0; l < nl; l++)
+        if (leaf_rows[l] >= n_rows) return fail(PCSF_EINVAL, "pcsf_bls_columns: leaf row out of range");
+    std::vector<int> below(n);
+    for (int64_t c = 0; c < len; c++) {
+        std::fill(below.begin(), below.end(), 0);
+        for (int l = 0; l < nl; l++) {
+            const int r = leaf_rows[l];
+            if (r < 0) continue;
+            const char x = rows[r][c];
+            below[l] = (x == '-' || x == '.' || x == 'N') ? 0 : 1;
+        }
+        for (int i = 0; i < n - 1; i++) below[parent[i]] += below[i];   // children precede parents
+        const int total = below[n - 1];
+        double t = 0.0;
+        for (int i = 0; i < n - 1; i++)
+            if (below[i] > 0 && below[i] < total) t += branch[i];
+        out[c] = t;
+    }
+    return PCSF_OK;
+}
+
 int pcsf_pack_regions(int32_t n_leaves, const int32_t *leaf_rows, int32_t n_rows, const char *const *rows_fwd,
                       const char *const *rows_rc, int64_t len, int32_t n_regions, const int32_t *rc,
                       const int64_t *lo, const int64_t *hi, int64_t *col_offsets, uint8_t *leaves)

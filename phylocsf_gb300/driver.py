@@ -11,6 +11,8 @@ that yields no region becomes a ``failure`` line, as in the reference.
 """
 from __future__ import annotations
 
+import ctypes
+
 from dataclasses import dataclass, field
 from typing import List, Optional, Tuple
 
@@ -78,33 +80,37 @@ def translate(dna: str) -> str:
     return "".join(out)
 
 
-def bls(tree: E.Tree, aln: List[str], leaf_rows: List[Optional[int]], lo: int, hi: int) -> float:
-    """Branch length score of nucleotide columns lo..hi (src/PhyloCSF.ml:252-262).
+def bls_columns(tree: E.Tree, aln: List[str], leaf_rows: List[Optional[int]]) -> np.ndarray:
+    """Per nucleotide column, the total length of the smallest subtree spanning the species
+    present there (Newick.subtree + Newick.total_length, lib/CamlPaml/Newick.ml:34-61), computed
+    once per alignment by the native helper pcsf_bls_columns."""
+    lib = E.load_library()
+    L = len(aln[0]) if aln else 0
+    out = np.zeros(L)
+    rows = (ctypes.c_char_p * max(len(aln), 1))(*[r.encode() for r in aln])
+    lr = np.array([-1 if r is None else r for r in leaf_rows], np.int32)
+    E._check(lib.pcsf_bls_columns(tree.nl, E._p(tree.parent, ctypes.c_int32), E._p(tree.branch, ctypes.c_double),
+                                  E._p(lr, ctypes.c_int32), len(aln), rows, L,
+                                  E._p(out, ctypes.c_double) if L else None))
+    return out
 
-    Per column, the reference takes Newick.subtree over the species present in
-    that column (not '-', '.', 'N') and its total length without the root branch
-    (Newick.ml:34-61): the length of the smallest subtree spanning those species.
-    An edge above node v belongs to it exactly when some but not all of the
-    present species lie below v.  The sum over columns is divided by the full
-    tree's length times the column count.
-    """
-    n, nl = tree.n, tree.nl
-    ncol = hi - lo + 1
-    pres = np.zeros((ncol, nl), np.int32)
-    for l in range(nl):
-        r = leaf_rows[l]
-        if r is None:
-            continue
-        row = np.frombuffer(aln[r][lo:hi + 1].encode(), np.uint8)
-        pres[:, l] = ~np.isin(row, np.frombuffer(b"-.N", np.uint8))
-    below = np.zeros((ncol, n), np.int32)
-    below[:, :nl] = pres
-    for i in range(n - 1):                      # children precede parents in T order
-        below[:, tree.parent[i]] += below[:, i]
-    total = below[:, n - 1:n]
-    inside = (below[:, : n - 1] > 0) & (below[:, : n - 1] < total)
-    bl_total = float((inside * tree.branch[None, : n - 1]).sum())
-    return bl_total / (float(tree.branch[: n - 1].sum()) * ncol)
+
+class BLS:
+    """Branch length score of nucleotide columns lo..hi (src/PhyloCSF.ml:252-262): the mean over
+    the columns of the spanning-subtree length, over the full tree's length.  The per-column
+    lengths are computed once; each region's score is a difference of prefix sums."""
+
+    def __init__(self, tree: E.Tree, aln: List[str], leaf_rows: List[Optional[int]]):
+        self.cum = np.concatenate([[0.0], np.cumsum(bls_columns(tree, aln, leaf_rows))])
+        self.total = float(tree.branch[: tree.n - 1].sum())
+
+    def __call__(self, lo: int, hi: int) -> float:
+        return (self.cum[hi + 1] - self.cum[lo]) / (self.total * (hi - lo + 1))
+
+
+def bls(tree: E.Tree, aln: List[str], leaf_rows: List[Optional[int]], lo: int, hi: int) -> float:
+    """Branch length score of nucleotide columns lo..hi of one alignment (src/PhyloCSF.ml:252-262)."""
+    return BLS(tree, aln, leaf_rows)(lo, hi)
 
 
 @dataclass
@@ -172,6 +178,8 @@ def process_alignment(engine: E.Engine, text: str, opts: Options, fn: str = "") 
         out.lines.append("%s\tfailure\tFailure(\"no regions successfully evaluated\")" % name)
         return out
 
+    bls_of = {}   # per strand: per-column spanning-subtree lengths, computed once
+
     def line(ty, rs: RegionScore):
         s = "%s\t%s\t%.4f" % (name, ty, rs.result["score"])
         if opts.frames != 1 or opts.orf_mode.lower() != "asis":
@@ -179,7 +187,10 @@ def process_alignment(engine: E.Engine, text: str, opts: Options, fn: str = "") 
         if six:
             s += "\t" + ("-" if rs.rc else "+")
         if opts.bls:
-            s += "\t%.4f" % bls(tree, rc_aln if rs.rc else aln, leaf_rows, rs.lo, rs.hi)
+            key = "rc" if rs.rc else "fwd"
+            if key not in bls_of:
+                bls_of[key] = BLS(tree, rc_aln if rs.rc else aln, leaf_rows)
+            s += "\t%.4f" % bls_of[key](rs.lo, rs.hi)
         if opts.anc_comp:
             s += "\t%.4f" % rs.result["anc_comp_score"]
         refdna = (rc_aln if rs.rc else aln)[0][rs.lo:rs.hi + 1]

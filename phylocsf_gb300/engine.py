@@ -126,6 +126,8 @@ SIGNATURES = {
     "pcsf_node_posteriors": ([_VP, _VP, ctypes.c_int32, _D, ctypes.c_int32, _I32, _D, _I32], ctypes.c_int),
     "pcsf_lpr_noalloc": ([_VP, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, _I64, ctypes.c_void_p, ctypes.c_void_p,
                           ctypes.c_void_p], ctypes.c_int),
+    "pcsf_bls_columns": ([ctypes.c_int32, _I32, _D, _I32, ctypes.c_int32, ctypes.POINTER(ctypes.c_char_p),
+                          ctypes.c_int64, _D], ctypes.c_int),
     "pcsf_simulate": ([ctypes.c_int32, _I32, ctypes.c_int32, _D, _D, ctypes.c_int32, _I64, _I32, _D, ctypes.c_int32,
                        ctypes.c_uint64, ctypes.c_int32, _U8], ctypes.c_int),
 }

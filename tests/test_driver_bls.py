@@ -50,3 +50,38 @@ def test_bls_matches_newick_subtree_restatement():
     want = tot / (_total(nt) * (hi - lo + 1))
     et = E.Tree(tree.parent, tree.branch, tree.labels)
     assert abs(D.bls(et, aln, rows, lo, hi) - want) < 1e-12
+
+
+def test_bls_prefix_sums_match_restatement_on_many_windows():
+    """The per-column spanning-subtree lengths (native pcsf_bls_columns) and the prefix-sum
+    windows against the per-column Newick.subtree restatement, on both strands of an example with
+    extra random gaps, for 40 random windows."""
+    tree, *_ = H.fixture_params("29mammals")
+
+    def mk(i):
+        if i < tree.nl:
+            return O.NewickNode([], tree.labels[i], float(tree.branch[i]))
+        return O.NewickNode([mk(tree.lchild[i]), mk(tree.rchild[i])], "", float(tree.branch[i]) if i < tree.n - 1 else None)
+    nt = mk(tree.n - 1)
+    ex = H.examples()["ALDH2.exon5.fa"]
+    sp = ex["species"]
+    rng = np.random.default_rng(5)
+    aln = ["".join(c if rng.random() > 0.15 else rng.choice(list("-.N")) for c in r) for r in ex["rows"]]
+    rows = O.leaf_rows_for(tree, sp)
+    which = {s: i for i, s in enumerate(sp)}
+    et = E.Tree(tree.parent, tree.branch, tree.labels)
+    comp = str.maketrans("ACGTacgt", "TGCAtgca")
+    for strand in (aln, [r.translate(comp)[::-1] for r in aln]):
+        per_col = D.bls_columns(et, strand, rows)
+        L = len(strand[0])
+        for i in range(0, L, 7):
+            st = _subtree(nt, lambda s: s in which and strand[which[s]][i] not in "-.N")
+            assert abs(per_col[i] - (_total(st) if st is not None else 0.0)) < 1e-12
+        b = D.BLS(et, strand, rows)
+        for _ in range(20):
+            lo = int(rng.integers(0, L - 1))
+            hi = int(rng.integers(lo, L))
+            want = sum(_total(s) if s is not None else 0.0 for s in
+                       (_subtree(nt, lambda x, i=i: x in which and strand[which[x]][i] not in "-.N")
+                        for i in range(lo, hi + 1))) / (_total(nt) * (hi - lo + 1))
+            assert abs(b(lo, hi) - want) < 1e-12
