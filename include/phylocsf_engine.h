@@ -124,7 +124,8 @@ typedef struct {
     int64_t kind_columns[5];     /* codon-column evaluations (columns x requests)  */
     double kind_ms[5];           /* device time (these sum to prune_ms)            */
     int32_t prune_grid;     /* launch configuration (not counters): CTAs of the SIMT pruning kernel, */
-    int32_t tc_grid;        /* and of the tensor-core kernel (0 if the engine has none)              */
+    int32_t tc_grid;        /* and of the tensor-core kernel (0 if the engine has none),             */
+    int32_t simt_tile;      /* and the SIMT kernel's column tile                                     */
 } pcsf_stats;
 
 /* ---------------------------------------------------------------- engine */
@@ -175,6 +176,16 @@ int pcsf_engine_set_exact_threshold(pcsf_engine *e, int64_t units);
 /* 1 if the engine has the float-float kernel (FP32 and tensor-core engines whose
  * tree fits its shared memory), else 0. */
 int pcsf_engine_exact_available(const pcsf_engine *e);
+
+/* Autotuner of the column tile of the compensated FP32 kernel (the returned values
+ * and the accurate search decisions).  Each candidate tile (32 and 64 columns, with
+ * the CTAs per SM its shared memory allows) is timed on the engine's stream over up
+ * to 256 regions of the batch at evenly spaced length quantiles (both models,
+ * rho = 1, one warm-up and two timed passes each); the fastest is kept for every
+ * later call on this engine and written to *tile (may be NULL).  The choice depends
+ * on the tree (partial slots and leaves) and the precision.  The FP64 engine has one
+ * tile (32) and keeps it.  No reference counterpart (the reference has no device). */
+int pcsf_engine_autotune(pcsf_engine *e, pcsf_batch *b, int32_t *tile);
 
 /* The CUDA stream (a cudaStream_t) on which the engine launches all of its
  * work, so that callers can time it with events on that stream.  No reference

@@ -162,6 +162,8 @@ struct pcsf_engine {
     HostBuf<int32_t> hwib, hstatus;
     HostBuf<double> hlpr, helpr;
     int prune_grid = 0;
+    int simt_tile = 0;             // SIMT column tile (0: the default rule; set by pcsf_engine_autotune)
+    int smem_sm = 0;               // shared memory per SM, for the grid of a tile
     int ff_grid = 0;               // CTAs of the float-float kernel (0: the tree does not fit it)
     // returned values (and the accurate search decisions) of a region come from the
     // float-float kernel when columns x (n_leaves - 2) reaches this; FP32 and tensor-core
@@ -544,6 +546,14 @@ static int setup_models(pcsf_engine *e, const double *Q[2], const double *eq[2],
     return PCSF_OK;
 }
 
+// CTAs of the SIMT kernel for a column tile: as many per SM as shared memory allows (<= 8)
+static int simt_grid(const pcsf_engine *e, int tile)
+{
+    const size_t smem = prune_smem_bytes(e->prec, e->nslots, e->nl, (int)e->sched.size(), tile);
+    int per_sm = std::max(1, (int)((size_t)e->smem_sm / (smem + 1024)));
+    return e->sm_count * std::min(per_sm, 8);
+}
+
 static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t flags)
 {
     int prec = flags & 0xff;
@@ -601,9 +611,8 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
     if (smem > (size_t)prop.sharedMemPerBlockOptin)
         return e->fail(PCSF_EINVAL, "tree needs %d partial slots (%zu B shared memory > %zu)", e->nslots, smem,
                        (size_t)prop.sharedMemPerBlockOptin);
-    int per_sm = std::max(1, (int)(prop.sharedMemPerMultiprocessor / (smem + 1024)));
-    per_sm = std::min(per_sm, 8);
-    e->prune_grid = prop.multiProcessorCount * per_sm;
+    e->smem_sm = (int)prop.sharedMemPerMultiprocessor;
+    e->prune_grid = simt_grid(e, 0);
     size_t gsmem = grad_smem_bytes(e->prec, e->nslots, e->nl, (int)e->sched.size(), 0);
     if (gsmem > (size_t)prop.sharedMemPerBlockOptin)
         return e->fail(PCSF_EINVAL, "tree needs %zu B shared memory for the gradient", gsmem);
@@ -667,7 +676,8 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     const bool tc = tc_prec(e->prec) && !accurate;
     // the gradient always runs the SIMT adjoint kernel (64-column tiles in FP32)
     const int TC = grad ? (e->prec == PCSF_PREC_FP64 ? 32 : 64)
-                        : ff ? ff_tile_cols() : !tc ? simt_tile_cols(e->prec, e->nslots) : prune_tile_cols(e->prec);
+                        : ff ? ff_tile_cols() : !tc ? simt_tile_cols(e->prec, e->nslots, e->simt_tile)
+                                                    : prune_tile_cols(e->prec);
     const int comp = (accurate && tc_prec(e->prec)) ? e->accurate_comp()
                                                                                               : e->comp_mode();
 
@@ -839,6 +849,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         pa.nbop = nbop;
         pa.dither = e->prec != PCSF_PREC_FP64;
         pa.dlo = dlo;
+        pa.tile = e->simt_tile;
         if (grad) {
             GradArgs ga{};
             ga.wi = pa.wi;
@@ -1690,6 +1701,7 @@ int pcsf_internal_noalloc_ctx(pcsf_engine *e, NoallocCtx *c)
     c->sched = e->dsched.p;
     c->m = e->dm;
     c->prune_grid = e->prune_grid;
+    c->simt_tile = e->simt_tile;
     c->ff_grid = e->prec != PCSF_PREC_FP64 ? e->ff_grid : 0;
     c->exact_min_units = e->exact_min_units;
     c->derr = e->derr.p;
@@ -2344,6 +2356,65 @@ int pcsf_engine_get_stats(const pcsf_engine *e, pcsf_stats *out)
     *out = e->stats;
     out->prune_grid = e->prune_grid;
     out->tc_grid = e->tc_grid;
+    out->simt_tile = simt_tile_cols(e->prec, e->nslots, e->simt_tile);
+    return PCSF_OK;
+}
+
+int pcsf_engine_autotune(pcsf_engine *e, pcsf_batch *b, int32_t *tile)
+{
+    if (!e) return PCSF_EINVAL;
+    if (!e->has_models) return e->fail(PCSF_EINVAL, "this engine has no coding / noncoding models");
+    CK(cudaSetDevice(e->device), "cudaSetDevice");
+    if (!b || b->e != e) return e->fail(PCSF_EINVAL, "pcsf_engine_autotune: batch does not belong to this engine");
+    if (e->prec == PCSF_PREC_FP64 || b->nreg == 0) {
+        if (tile) *tile = simt_tile_cols(e->prec, e->nslots, e->simt_tile);
+        return PCSF_OK;
+    }
+    // up to 256 regions at evenly spaced length quantiles, both models at rho = 1
+    std::vector<int> order(b->nreg);
+    for (int r = 0; r < b->nreg; r++) order[r] = r;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return b->offs[x + 1] - b->offs[x] < b->offs[y + 1] - b->offs[y]; });
+    const int ns = std::min(b->nreg, 256);
+    std::vector<Request> reqs;
+    for (int k = 0; k < ns; k++) {
+        const int r = order[(size_t)k * (b->nreg - 1) / std::max(ns - 1, 1)];
+        for (int m = 0; m < 2; m++) reqs.push_back(Request{r, m, 0, 0, 1.0});
+    }
+    const int saved_tile = e->simt_tile, saved_grid = e->prune_grid;
+    const int64_t saved_exact = e->exact_min_units;
+    const pcsf_stats saved_stats = e->stats;
+    e->exact_min_units = INT64_MAX;   // time the FP32 kernel on every sampled region
+    int best = 0;
+    double best_ms = 1e300;
+    int rc = PCSF_OK;
+    for (int cand : {64, 32}) {
+        if (prune_smem_bytes(e->prec, e->nslots, e->nl, (int)e->sched.size(), cand) > e->smem_optin) continue;
+        e->simt_tile = cand;
+        e->prune_grid = simt_grid(e, cand);
+        double ms = 0.0;
+        std::vector<Eval> res;
+        for (int it = 0; it < 3 && rc == PCSF_OK; it++) {
+            const double before = e->stats.kind_ms[0];
+            rc = evaluate(e, b, reqs, res, nullptr, true);
+            if (it > 0) ms += e->stats.kind_ms[0] - before;
+        }
+        if (rc != PCSF_OK) break;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = cand;
+        }
+    }
+    e->exact_min_units = saved_exact;
+    e->stats = saved_stats;
+    if (rc != PCSF_OK || best == 0) {
+        e->simt_tile = saved_tile;
+        e->prune_grid = saved_grid;
+        return rc != PCSF_OK ? rc : e->fail(PCSF_EINVAL, "pcsf_engine_autotune: no tile fits this tree");
+    }
+    e->simt_tile = best;
+    e->prune_grid = simt_grid(e, best);
+    if (tile) *tile = best;
     return PCSF_OK;
 }
 

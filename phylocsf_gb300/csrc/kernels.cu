@@ -643,16 +643,18 @@ int prune_tile_cols(int prec)
 // Column tile of the SIMT pruning kernel.  FP32 uses 64 columns, except for trees of
 // five or more partial slots (the 120-leaf tree): there 64 columns take ~124 KB of
 // shared memory, one CTA per SM, and 32 columns let two CTAs share an SM.
-int simt_tile_cols(int prec, int nslots)
+// tile (32 or 64) overrides this rule for the FP32 kernel (the engine's autotuner sets it).
+int simt_tile_cols(int prec, int nslots, int tile)
 {
     if (prec == PCSF_PREC_FP64) return 32;
+    if (tile == 32 || tile == 64) return tile;
     return nslots >= 5 ? 32 : 64;
 }
 
-size_t prune_smem_bytes(int prec, int nslots, int nl, int nint)
+size_t prune_smem_bytes(int prec, int nslots, int nl, int nint, int tile)
 {
     if (prec == PCSF_PREC_FP64) return PruneSmem<double, 32>::bytes(nslots, nl, nint);
-    if (simt_tile_cols(prec, nslots) == 32) return PruneSmem<float, 32>::bytes(nslots, nl, nint);
+    if (simt_tile_cols(prec, nslots, tile) == 32) return PruneSmem<float, 32>::bytes(nslots, nl, nint);
     return PruneSmem<float, 64>::bytes(nslots, nl, nint);
 }
 
@@ -670,7 +672,7 @@ cudaError_t launch_prune(int prec, int comp, const PruneArgs &a, cudaStream_t s,
 {
     if (a.nwi <= 0) return cudaSuccess;
     if (prec == PCSF_PREC_FP64) return launch_prune_t<double, 32, 0>(a, s, grid);
-    if (simt_tile_cols(prec, a.nslots) == 32) {
+    if (simt_tile_cols(prec, a.nslots, a.tile) == 32) {
         if (comp == 1) return launch_prune_t<float, 32, 1>(a, s, grid);
         if (comp == 2) return launch_prune_t<float, 32, 2>(a, s, grid);
         return launch_prune_t<float, 32, 0>(a, s, grid);

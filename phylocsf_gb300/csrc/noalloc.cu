@@ -104,7 +104,7 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
     // columns x (n_leaves - 2) reach the engine's threshold -- the float-float kernel on
     // the FP64 P(t)
     const int prec = cx.prec;
-    const int TC = simt_tile_cols(prec, cx.nslots);
+    const int TC = simt_tile_cols(prec, cx.nslots, cx.simt_tile);
     const int TCX = ff_tile_cols();
     const bool fp32 = prec != PCSF_PREC_FP64;
     const size_t es = fp32 ? 4 : 8;
@@ -206,6 +206,7 @@ extern "C" int pcsf_lpr_noalloc(pcsf_engine *e, int32_t model, double rho, int32
     pa.nbr = cx.nbr;
     pa.nslots = cx.nslots;
     pa.m = cx.m;
+    pa.tile = cx.simt_tile;
     if (ce == cudaSuccess && nws) {
         pa.wi = d_wi;
         pa.nwi = nws;

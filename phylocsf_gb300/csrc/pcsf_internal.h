@@ -115,12 +115,13 @@ struct PruneArgs {
     int nbop;                //   of the branches above internal nodes (node nl + k)
     int dither;              // SIMT FP32 kernel: per-column dithering of the leaf partials (prune_common.cuh)
     const float *dlo;        // SIMT FP32 kernel, may be null: per chunk-local P set [nbr][K] low parts of diag(E)
+    int tile;                // SIMT FP32 kernel: column tile 32 or 64, 0 = the default rule (simt_tile_cols)
 };
 // comp: 0 plain FP32 sums, 1 Kahan, 2 blocked Kahan (see prune_common.cuh)
 cudaError_t launch_prune(int prec, int comp, const PruneArgs &a, cudaStream_t s, int grid);
 int prune_tile_cols(int prec);
-int simt_tile_cols(int prec, int nslots);   // the SIMT kernel's column tile (k_prune)
-size_t prune_smem_bytes(int prec, int nslots, int nl, int nint);
+int simt_tile_cols(int prec, int nslots, int tile = 0);   // the SIMT kernel's column tile (k_prune)
+size_t prune_smem_bytes(int prec, int nslots, int nl, int nint, int tile = 0);
 
 // Adjoint gradient over work items (grad_kernels.cu): per work item the lpr /
 // elpr partials and d lpr / d t_c for every branch c.
@@ -237,6 +238,7 @@ struct NoallocCtx {
     const SchedNode *sched;
     DevModels m;
     int prune_grid;
+    int simt_tile;         // SIMT column tile chosen for the engine (0: the default rule)
     int ff_grid;           // CTAs of the float-float kernel (0: not available)
     int64_t exact_min_units;   // regions with columns x (nl - 2) >= this use the float-float kernel
     int *derr;             // device error flag of timed-out waits

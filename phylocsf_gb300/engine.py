@@ -82,7 +82,7 @@ class Stats(ctypes.Structure):
                 ("prune_launches", ctypes.c_int64), ("pform_launches", ctypes.c_int64),
                 ("kind_launches", ctypes.c_int64 * 5), ("kind_columns", ctypes.c_int64 * 5),
                 ("kind_ms", ctypes.c_double * 5),
-                ("prune_grid", ctypes.c_int32), ("tc_grid", ctypes.c_int32)]
+                ("prune_grid", ctypes.c_int32), ("tc_grid", ctypes.c_int32), ("simt_tile", ctypes.c_int32)]
 
 
 # Every entry point declared in include/*.h, with its ctypes signature.
@@ -121,6 +121,7 @@ SIGNATURES = {
                            _U8], ctypes.c_int),
     "pcsf_engine_set_exact_threshold": ([_VP, ctypes.c_int64], ctypes.c_int),
     "pcsf_engine_exact_available": ([_VP], ctypes.c_int),
+    "pcsf_engine_autotune": ([_VP, _VP, _I32], ctypes.c_int),
     "pcsf_branch_counts": ([_VP, _VP, ctypes.c_int32, _D, _D, _D, _I32], ctypes.c_int),
     "pcsf_ell": ([_VP, ctypes.c_int32, ctypes.c_double, _D, _D], ctypes.c_int),
     "pcsf_node_posteriors": ([_VP, _VP, ctypes.c_int32, _D, ctypes.c_int32, _I32, _D, _I32], ctypes.c_int),
@@ -505,6 +506,13 @@ class Engine:
         """Regions with columns x (n_leaves - 2) >= units take their returned values from the
         float-float kernel (0: all regions)."""
         _check(self.lib.pcsf_engine_set_exact_threshold(self.handle, int(units)), self.handle)
+
+    def autotune(self, batch: Batch) -> int:
+        """Time the compensated FP32 kernel's column tiles on a sample of the batch, keep the
+        fastest for this engine; returns the chosen tile."""
+        t = ctypes.c_int32()
+        _check(self.lib.pcsf_engine_autotune(self.handle, batch.handle, ctypes.byref(t)), self.handle)
+        return t.value
 
     @property
     def exact_available(self) -> bool:

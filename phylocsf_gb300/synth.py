@@ -233,3 +233,53 @@ def workload_120mammals_fixed(total_cols: int = 2_000_000, seed: int = 0) -> Wor
 
 def workload_100vertebrates_mle(n_regions: int = 20000, seed: int = 0) -> Workload:
     return realize(spec_100vertebrates_mle(n_regions, seed))
+
+
+_NT = np.frombuffer(b"ACGT", np.uint8)
+
+
+def nucleotide_rows(codes: np.ndarray, ref_leaf: int = 0) -> list:
+    """Codon-level leaf codes [L][nl] -> nl nucleotide rows of 3L characters: codon
+    16 n1 + 4 n2 + n3 as its three bases, a marginalised codon as '---' (as 'NNN' in the
+    reference row, which the driver requires ungapped)."""
+    L, nl = codes.shape
+    c = codes.astype(np.int64)
+    nt = np.empty((nl, L, 3), np.uint8)
+    ok = c < 64
+    for k, sh in enumerate((4, 2, 0)):
+        nt[:, :, k] = np.where(ok, _NT[(np.where(ok, c, 0) >> sh) & 3], ord("-")).T
+    nt[ref_leaf][~ok[:, ref_leaf]] = ord("N")
+    return [nt[l].tobytes().decode() for l in range(nl)]
+
+
+def workload_100vertebrates_6frame(n_regions: int = 20000, seed: int = 0, min_codons: int = 25) -> Workload:
+    """Six-frame scoring on 100vertebrates (the batching configuration): alignments of
+    log-uniform 30-10,000 codons simulated from the coding / noncoding ECMs at 1:3 with
+    5-40% gaps per species, written out as nucleotide rows; every alignment's candidate
+    regions in all six frames (AsIs: each frame's whole length) are enumerated and packed
+    by the native pcsf_candidate_regions / pcsf_pack_regions, the MFA driver's path
+    (src/PhyloCSF.ml:134-246).  Regions of one alignment are consecutive."""
+    ps = load_params("100vertebrates")
+    nl = ps.tree.nl
+    rng = np.random.default_rng(seed)
+    n_aln = max(1, -(-n_regions // 6))
+    lengths = log_uniform_lengths(rng, n_aln, 30, 10000)
+    models = (rng.random(n_aln) >= 0.25).astype(np.int32)
+    gf = gap_fractions(rng, n_aln, nl, 0.05, 0.40, 0.0)
+    aoffs, codes = simulate(ps, lengths, models, gf, seed)
+    comp = str.maketrans("ACGTN-", "TGCAN-")
+    all_offs, all_leaves, region_models = [np.zeros(1, np.int64)], [], []
+    base = 0
+    for a in range(n_aln):
+        rows = nucleotide_rows(codes[aoffs[a]:aoffs[a + 1]])
+        rows_rc = [r.translate(comp)[::-1] for r in rows]
+        regs = E.candidate_regions(rows[0], 6, "AsIs", min_codons)
+        o, lv = E.pack_regions(nl, list(range(nl)), rows, rows_rc, regs)
+        all_offs.append(o[1:] + base)
+        all_leaves.append(lv)
+        region_models.extend([models[a]] * len(regs))
+        base += int(o[-1])
+    offs = np.concatenate(all_offs)
+    leaves = np.concatenate(all_leaves) if all_leaves else np.zeros((0, nl), np.uint8)
+    return Workload("100vertebrates_6frame_%dregions" % (len(offs) - 1), ps, offs, leaves,
+                    np.array(region_models, np.int32), E.MLE)

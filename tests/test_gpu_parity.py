@@ -277,3 +277,22 @@ def test_stats_count_kernels():
     s = e.stats()
     assert s["kernel_launches"] >= 3 and s["evaluations"] == 4
     assert s["column_branches"] == 300 * 2 * (2 * 12 - 2)
+
+
+@pytest.mark.parametrize("name,prec", [("58mammals", "fp32b"), ("120mammals", "tf32x3b")])
+def test_autotune_keeps_values(name, prec):
+    """pcsf_engine_autotune picks one of the FP32 kernel's column tiles by timing and reports it;
+    the per-column arithmetic does not depend on the tile, so lpr changes only by the order of the
+    FP64 tile sums (<= 1e-12 relative)."""
+    ps = synth.load_params(name)
+    e = P.Engine(ps.tree, ps.S_c, ps.pi_c, ps.S_n, ps.pi_n, precision=prec)
+    offs, leaves = _synthetic(name, [30, 64, 65, 400, 900], seed=13)
+    b = e.batch(offs, leaves)
+    before = [e.lpr(b, m, 0.7)[0] for m in (0, 1)]
+    tile = e.autotune(b)
+    assert tile in (32, 64)
+    assert e.stats()["simt_tile"] == tile
+    after = [e.lpr(b, m, 0.7)[0] for m in (0, 1)]
+    for x, y in zip(before, after):
+        np.testing.assert_allclose(y, x, rtol=1e-12, atol=0)
+    e.close()

@@ -34,3 +34,23 @@ def test_workload_spec_regions_match_realized_workload():
                                     spec.seed, sub)
     want = np.concatenate([wl.leaves[wl.col_offsets[r]:wl.col_offsets[r + 1]] for r in sub])
     assert np.array_equal(got, want)
+
+
+def test_nucleotide_rows_round_trip_through_native_packing():
+    """Simulated codon columns written out as nucleotide rows and packed back by the native
+    region packer (pleaves' path) give the same leaf codes in frame 0 of the forward strand;
+    the six AsIs frames of an alignment cover its whole length."""
+    from phylocsf_gb300 import engine as E
+    ps = synth.load_params("12flies")
+    rng = np.random.default_rng(4)
+    gf = synth.gap_fractions(rng, 1, ps.tree.nl, 0.1, 0.3, 0.0)
+    offs, codes = synth.simulate(ps, np.array([90]), np.array([0], np.int32), gf, seed=2)
+    rows = synth.nucleotide_rows(codes)
+    assert all(len(r) == 270 for r in rows) and "-" not in rows[0]
+    comp = str.maketrans("ACGTN-", "TGCAN-")
+    rc_rows = [r.translate(comp)[::-1] for r in rows]
+    regs = E.candidate_regions(rows[0], 6, "AsIs", 25)
+    assert len(regs) == 6 and sorted(r[0] for r in regs) == [False] * 3 + [True] * 3
+    o, lv = E.pack_regions(ps.tree.nl, list(range(ps.tree.nl)), rows, rc_rows, regs)
+    k = [i for i, r in enumerate(regs) if not r[0] and r[1] == 0][0]
+    assert np.array_equal(lv[o[k]:o[k + 1]], codes)
