@@ -572,6 +572,89 @@ def run_ours(args, world, rank, local):
     eng.close()
 
 
+def run_omega(args, world, rank, local):
+    """The differentiation configuration: the OmegaModel gradient with respect to every branch
+    length, rho, kappa and omega for alignments of 200-2,000 codons on 100vertebrates simulated at
+    per-alignment omega; one step = one pcsf_omega_grad over the whole batch."""
+    import torch
+    import phylocsf_gb300 as P
+    from phylocsf_gb300 import synth, omega_fit
+    wl = synth.workload_100vertebrates_omega(n_alignments=args.regions, seed=rank)
+    prec = args.precision if args.precision != "tf32x3b" else "fp32b"
+    eng = P.Engine.for_tree(wl.tree, precision=prec, device=local)
+    stream = torch.cuda.ExternalStream(eng.stream_handle(), device=torch.device("cuda", local))
+    b = eng.batch(wl.col_offsets, wl.leaves)
+    for _ in range(args.warmup):
+        g = eng.omega_grad(b, wl.kappa, wl.omega, 1.0, wl.sigma)
+    clocks = ClockSampler(local) if rank == 0 else None
+    barrier(world)
+    torch.cuda.synchronize(local)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        g = eng.omega_grad(b, wl.kappa, wl.omega, 1.0, wl.sigma)
+    e1.record(stream)
+    e1.synchronize()
+    barrier(world)
+    ms = max_over_ranks(e0.elapsed_time(e1), world)
+    clk = clocks.stop() if clocks else None
+    value = world * wl.n_regions * args.steps / (ms / 1000.0)
+    nbr = wl.tree.n - 1
+    line = {"metric": "OmegaModel gradient (every branch, rho, kappa, omega): alignments/s", "value": value,
+            "unit": "alignments/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": DTYPES.get(prec, prec) + ", P(t) and its eigenbasis derivative f64", "data": DATA,
+            "config": {"workload": wl.name, "tree": "100vertebrates", "alignments_per_gpu": wl.n_regions,
+                       "columns_per_gpu": wl.total_cols, "gradient_entries_per_alignment": nbr + 3,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (%.0f MB)" % (wl.leaves.nbytes / 1e6)},
+            "column_branches_per_s": world * wl.total_cols * nbr * args.steps / (ms / 1000.0),
+            "clocks": clk}
+    if rank == 0:
+        # against the FP64 engine on alignments at evenly spaced length quantiles
+        sub = stratified(wl.col_offsets, args.fp64_regions)
+        parts = [wl.leaves[wl.col_offsets[i]:wl.col_offsets[i + 1]] for i in sub]
+        so = np.zeros(len(sub) + 1, np.int64)
+        so[1:] = np.cumsum([x.shape[0] for x in parts])
+        e64 = P.Engine.for_tree(wl.tree, precision="fp64", device=local)
+        b64 = e64.batch(so, np.concatenate(parts))
+        t0 = time.perf_counter()
+        g64 = e64.omega_grad(b64, wl.kappa, wl.omega[sub], 1.0, wl.sigma)
+        t64 = time.perf_counter() - t0
+        rel = {}
+        for k in ("d_kappa", "d_omega", "d_rho", "d_branch"):
+            a, c = g64[k], g[k][sub]
+            rel[k] = float(np.max(np.abs(c - a) / (np.abs(a) + 1e-2)))
+        line["accuracy"] = {"vs_fp64_gpu": {"alignments": int(len(sub)), "max_rel_error": rel,
+                                            "lpr_max_rel": float(np.max(np.abs(g["lpr"][sub] - g64["lpr"]) /
+                                                                        np.abs(g64["lpr"])))},
+                            "fp64_seconds_on_sample": t64}
+        # gradient MAP (rho, kappa at omega = 1) beside the reference's Brent coordinate ascent (H0)
+        bs = eng.batch(so, np.concatenate(parts))
+        t0 = time.perf_counter()
+        brent = eng.omega_score(bs)
+        tb = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        gm = omega_fit.gradient_map(eng, bs, omega=1.0, sigma=1.0)
+        tg = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        fo = omega_fit.gradient_map(eng, bs, sigma=1.0, fit_omega=True, iters=60)
+        to = time.perf_counter() - t0
+        gap = gm["objective"] - (brent["lpr_h0"] + omega_fit.log_prior_rho(brent["rho_h0"]))
+        L = np.diff(so)
+        line["fits"] = {"alignments": int(len(sub)),
+                        "brent_kr_map_seconds": tb, "brent_evaluations_mean": float(np.mean(brent["evals"])),
+                        "gradient_map_seconds": tg, "gradient_map_evaluations_mean": float(np.mean(gm["evals"])),
+                        "objective_gap_gradient_minus_brent": {"min": float(gap.min()), "max": float(gap.max())},
+                        "omega_mle_seconds": to,
+                        "omega_mle_log_ratio_to_simulated": {
+                            "median_abs": float(np.median(np.abs(np.log(fo["omega"] / wl.omega[sub])))),
+                            "median_abs_1000_codons_or_more": float(np.median(np.abs(
+                                np.log(fo["omega"][L >= 1000] / wl.omega[sub][L >= 1000])))) if (L >= 1000).any() else None}}
+        line["native_libs_loaded"] = loaded_native_libs()
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -602,6 +685,8 @@ def main():
     world, rank, local = dist_init()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "100vertebrates_omega":
+        run_omega(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

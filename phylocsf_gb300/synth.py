@@ -76,15 +76,22 @@ def p_matrices(S: np.ndarray, pi: np.ndarray, t: np.ndarray) -> np.ndarray:
 def simulate(ps: ParamSet, lengths: np.ndarray, models: np.ndarray, gap_frac: Optional[np.ndarray], seed: int,
              reject_stop_leaf0: bool = True, threads: int = 0, rho: float = 1.0):
     """Simulate regions: returns (col_offsets int64[R+1], leaves uint8[total, nl])."""
-    lib = E.load_library()
-    tree = ps.tree
     P, prior = simulation_inputs(ps, rho)
+    return simulate_with(ps.tree, P, prior, lengths, models, gap_frac, seed, reject_stop_leaf0, threads)
+
+
+def simulate_with(tree, P: np.ndarray, prior: np.ndarray, lengths: np.ndarray, models: np.ndarray,
+                  gap_frac: Optional[np.ndarray], seed: int, reject_stop_leaf0: bool = True, threads: int = 0):
+    """Simulate regions from explicit models: P [n_models][nbr][64][64], prior [n_models][64]."""
+    lib = E.load_library()
+    P = np.ascontiguousarray(P, np.float64)
+    prior = np.ascontiguousarray(prior, np.float64)
     offs = np.zeros(len(lengths) + 1, np.int64)
     offs[1:] = np.cumsum(lengths)
     leaves = np.empty((int(offs[-1]), tree.nl), np.uint8)
     models = np.ascontiguousarray(models, np.int32)
     gf = None if gap_frac is None else np.ascontiguousarray(gap_frac, np.float64)
-    rc = lib.pcsf_simulate(tree.nl, E._p(tree.parent, ctypes.c_int32), 2, E._p(P, ctypes.c_double),
+    rc = lib.pcsf_simulate(tree.nl, E._p(tree.parent, ctypes.c_int32), P.shape[0], E._p(P, ctypes.c_double),
                            E._p(prior, ctypes.c_double), len(lengths), E._p(offs, ctypes.c_int64),
                            E._p(models, ctypes.c_int32), None if gf is None else E._p(gf, ctypes.c_double),
                            1 if reject_stop_leaf0 else 0, seed, threads,
@@ -283,3 +290,88 @@ def workload_100vertebrates_6frame(n_regions: int = 20000, seed: int = 0, min_co
     leaves = np.concatenate(all_leaves) if all_leaves else np.zeros((0, nl), np.uint8)
     return Workload("100vertebrates_6frame_%dregions" % (len(offs) - 1), ps, offs, leaves,
                     np.array(region_models, np.int32), E.MLE)
+
+
+# ---------------------------------------------------------------- OmegaModel workloads
+_GENETIC_CODE = "KNKNTTTTRSRSIIMIQHQHPPPPRRRRLLLLEDEDAAAAGGGGVVVV*Y*YSSSS*CWCLFLF"
+_STOPS = (48, 50, 56)
+
+
+def omega_rate_matrix(kappa: float, omega: float, sigma: float = 1.0, f3x4: Optional[np.ndarray] = None):
+    """(Q, pi) of the OmegaModel's parametric codon model (src/OmegaModel.ml:21-80): F3x4 codon
+    frequencies (9 values, each position's A, C, G relative to T; default uniform) with the stop
+    codons' mass damped by sigma; q_ij = pi_j x kappa (transitions) x omega (non-synonymous) between
+    codons one nucleotide apart; Q scaled to mean rate 1."""
+    f = np.ones(9) if f3x4 is None else np.asarray(f3x4, np.float64)
+    nuc = np.array([[i // 16, (i // 4) % 4, i % 4] for i in range(64)])
+    rel = np.ones((3, 4))
+    rel[:, :3] = f.reshape(3, 3)
+    pos = rel / rel.sum(axis=1, keepdims=True)
+    sc = pos[0][nuc[:, 0]] * pos[1][nuc[:, 1]] * pos[2][nuc[:, 2]]
+    pi = sc / (1.0 - (1.0 - sigma) * sc[list(_STOPS)].sum())
+    diff = nuc[:, None, :] != nuc[None, :, :]
+    one = diff.sum(axis=2) == 1
+    a = np.where(diff, nuc[:, None, :], -1).max(axis=2)
+    b = np.where(diff, nuc[None, :, :], -1).max(axis=2)
+    transition = ((a == 0) & (b == 2)) | ((a == 2) & (b == 0)) | ((a == 1) & (b == 3)) | ((a == 3) & (b == 1))
+    aa = np.array(list(_GENETIC_CODE))
+    stop = np.isin(np.arange(64), _STOPS)
+    nonsyn = (~stop[:, None]) & (~stop[None, :]) & (aa[:, None] != aa[None, :])
+    Q = np.where(one, pi[None, :] * np.where(transition, kappa, 1.0) * np.where(nonsyn, omega, 1.0), 0.0)
+    np.fill_diagonal(Q, -Q.sum(axis=1))
+    return Q / (-(pi * np.diag(Q)).sum()), pi
+
+
+def p_matrices_q(Q: np.ndarray, pi: np.ndarray, t: np.ndarray) -> np.ndarray:
+    """P(t) of a reversible Q for each t (symmetrised eigensystem); rows clamped and renormalised."""
+    sq = np.sqrt(pi)
+    A = sq[:, None] * Q / sq[None, :]
+    lam, U = np.linalg.eigh(0.5 * (A + A.T))
+    out = np.empty((len(t), 64, 64))
+    for i, ti in enumerate(t):
+        M = (U * np.exp(lam * ti)) @ U.T
+        P = np.maximum(M * sq[None, :] / sq[:, None], 0.0)
+        out[i] = P / P.sum(1, keepdims=True)
+    return out
+
+
+@dataclass
+class OmegaWorkload:
+    name: str
+    tree: E.Tree
+    col_offsets: np.ndarray
+    leaves: np.ndarray
+    omega: np.ndarray        # per region, the omega it was simulated at
+    kappa: float
+    sigma: float
+
+    @property
+    def n_regions(self) -> int:
+        return len(self.col_offsets) - 1
+
+    @property
+    def total_cols(self) -> int:
+        return int(self.col_offsets[-1])
+
+
+def workload_100vertebrates_omega(n_alignments: int = 2000, seed: int = 0, n_omega: int = 16,
+                                  lengths: Optional[np.ndarray] = None) -> OmegaWorkload:
+    """The differentiation configuration: alignments of log-uniform 200-2,000 codons on
+    100vertebrates simulated under the OmegaModel at kappa = 2.5, sigma = 1, uniform F3x4 and
+    omega log-uniform in [0.05, 2] (n_omega levels), with 5-20 % gaps per species."""
+    ps = load_params("100vertebrates")
+    tree = ps.tree
+    rng = np.random.default_rng(seed)
+    L = log_uniform_lengths(rng, n_alignments, 200, 2000) if lengths is None else np.asarray(lengths, np.int64)
+    levels = np.exp(np.linspace(np.log(0.05), np.log(2.0), n_omega))
+    which = rng.integers(0, n_omega, size=len(L)).astype(np.int32)
+    gf = gap_fractions(rng, len(L), tree.nl, 0.05, 0.20, 0.0)
+    nbr = tree.n - 1
+    P = np.empty((n_omega, nbr, 64, 64))
+    prior = np.empty((n_omega, 64))
+    for k, w in enumerate(levels):
+        Q, pi = omega_rate_matrix(2.5, w, 1.0)
+        P[k] = p_matrices_q(Q, pi, tree.branch[:nbr])
+        prior[k] = pi / pi.sum()
+    offs, lv = simulate_with(tree, P, prior, L, which, gf, seed)
+    return OmegaWorkload("100vertebrates_omega_%dalignments" % len(L), tree, offs, lv, levels[which], 2.5, 1.0)

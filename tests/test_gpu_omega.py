@@ -133,3 +133,90 @@ def test_gradient_map_beside_brent():
     assert np.all(gap <= 0.5), gap
     assert np.allclose(gm["rho"], brent["rho_h0"], rtol=0.05)
     assert np.allclose(gm["kappa"], brent["kappa_h0"], rtol=0.05)
+
+
+# ---------------------------------------------------------------- the differentiation configuration
+# OmegaModel on the 100vertebrates tree, alignments simulated under the OmegaModel's own Q at
+# kappa = 2.5, sigma = 1, uniform F3x4 and omega log-uniform in [0.05, 2] (synth.workload_100vertebrates_omega).
+
+def _omega_wl(lengths, seed):
+    return synth.workload_100vertebrates_omega(seed=seed, lengths=np.asarray(lengths))
+
+
+def test_omega_grad_100vertebrates_finite_differences():
+    """d lpr / d {kappa, omega, rho} and d lpr / d t for a leaf branch, an internal branch and a root
+    branch, by pcsf_omega_grad (FP64 engine) against central differences with h = 1e-5 of the engine's
+    own lpr; per region omega (the value it was simulated at).  Within 1e-5 relative + 2e-3 absolute
+    (lpr here is ~1e5 nats, so the differences carry ~1e-6 of rounding over 2h)."""
+    wl = _omega_wl([200, 450, 800], seed=3)
+    tree = wl.tree
+    e = P.Engine.for_tree(tree, precision="fp64")
+    b = e.batch(wl.col_offsets, wl.leaves)
+    kappa, omega, rho, sigma, h = 2.2, wl.omega.copy(), 1.0, 1.0, 1e-5
+    g = e.omega_grad(b, kappa, omega, rho, sigma)
+    assert (g["status"] == 0).all()
+
+    def lpr_at(eng, bb, k, o, r):
+        return eng.omega_grad(bb, k, o, r, sigma, branches=False)["lpr"]
+
+    fd = {"d_kappa": (lpr_at(e, b, kappa + h, omega, rho) - lpr_at(e, b, kappa - h, omega, rho)) / (2 * h),
+          "d_omega": (lpr_at(e, b, kappa, omega + h, rho) - lpr_at(e, b, kappa, omega - h, rho)) / (2 * h),
+          "d_rho": (lpr_at(e, b, kappa, omega, rho + h) - lpr_at(e, b, kappa, omega, rho - h)) / (2 * h)}
+    for k, v in fd.items():
+        assert np.all(np.abs(g[k] - v) <= 1e-5 * np.abs(v) + 2e-3), (k, g[k], v)
+    for br in (0, tree.nl + 3, tree.n - 2):
+        vals = []
+        for sgn in (1, -1):
+            bl = tree.branch.copy()
+            bl[br] += sgn * h
+            t2 = P.Tree(tree.parent, bl, tree.labels)
+            e2 = P.Engine.for_tree(t2, precision="fp64")
+            vals.append(lpr_at(e2, e2.batch(wl.col_offsets, wl.leaves), kappa, omega, rho))
+            e2.close()
+        fdb = (vals[0] - vals[1]) / (2 * h)
+        assert np.all(np.abs(g["d_branch"][:, br] - fdb) <= 1e-5 * np.abs(fdb) + 2e-3), (br, g["d_branch"][:, br], fdb)
+    e.close()
+
+
+def test_omega_grad_100vertebrates_fp32_close_to_fp64():
+    """The configuration's arithmetic (FP32 with compensated sums, P(t) and its eigenbasis
+    derivative in FP64) against the FP64 engine: every gradient entry within 1e-3 relative + 1e-2."""
+    wl = _omega_wl([300, 900, 1500, 250], seed=5)
+    a = P.Engine.for_tree(wl.tree, precision="fp64")
+    c = P.Engine.for_tree(wl.tree, precision="fp32c")
+    ga = a.omega_grad(a.batch(wl.col_offsets, wl.leaves), 2.5, wl.omega, 1.1, 1.0)
+    gc = c.omega_grad(c.batch(wl.col_offsets, wl.leaves), 2.5, wl.omega, 1.1, 1.0)
+    for k in ("d_kappa", "d_omega", "d_rho", "d_branch"):
+        assert np.all(np.abs(gc[k] - ga[k]) <= 1e-3 * np.abs(ga[k]) + 1e-2), k
+    np.testing.assert_allclose(gc["lpr"], ga["lpr"], rtol=1e-7)
+    a.close()
+    c.close()
+
+
+def test_gradient_map_100vertebrates_beside_brent_and_omega_mle():
+    """On 100vertebrates: (a) the gradient MAP of (rho, kappa) at omega = 1 reaches at least the
+    objective of the reference's Brent coordinate ascent (the H0 fit of pcsf_omega_score) on every
+    region and lands next to it; (b) with omega free, the gradient fit of (rho, kappa, omega) ends
+    with a vanishing projected gradient and recovers the omega each 1,500-codon alignment was
+    simulated at (within a factor 1.35)."""
+    from phylocsf_gb300 import omega_fit
+    wl = _omega_wl([250, 600, 1500, 1500, 1500, 400], seed=7)
+    e = P.Engine.for_tree(wl.tree, precision="fp64")
+    b = e.batch(wl.col_offsets, wl.leaves)
+    brent = e.omega_score(b)
+    gm = omega_fit.gradient_map(e, b, omega=1.0, sigma=1.0)
+    assert (gm["status"] == 0).all()
+    brent_f = brent["lpr_h0"] + omega_fit.log_prior_rho(brent["rho_h0"])
+    gap = gm["objective"] - brent_f
+    print("100vertebrates gradient MAP - Brent objective:", gap, "evaluations:", gm["evals"], "Brent:", brent["evals"])
+    assert np.all(gap >= -1e-6 * np.abs(brent_f) - 1e-6), gap
+    assert np.allclose(gm["rho"], brent["rho_h0"], rtol=0.05)
+    assert np.allclose(gm["kappa"], brent["kappa_h0"], rtol=0.05)
+    fo = omega_fit.gradient_map(e, b, sigma=1.0, fit_omega=True, iters=60)
+    print("omega MLE:", fo["omega"], "simulated at:", wl.omega)
+    assert (fo["status"] == 0).all()
+    assert np.all(np.abs(fo["gradient"]).max(axis=1) <= 1e-3 * np.maximum(1.0, np.abs(fo["objective"])))
+    assert np.all(fo["objective"] >= gm["objective"] - 1e-6 * np.abs(gm["objective"]))
+    long = np.diff(wl.col_offsets) >= 1500
+    assert np.all(np.abs(np.log(fo["omega"][long] / wl.omega[long])) <= np.log(1.35)), (fo["omega"], wl.omega)
+    e.close()

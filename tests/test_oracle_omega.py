@@ -47,3 +47,15 @@ def test_omega_score_small():
     assert math.isfinite(sc) and 1.0 <= q0[0] <= 10.0 and 0.001 <= r0 <= 10.0
     assert q1[1] == 0.2 and q1[2] == 0.01
     assert evals > 20
+
+
+def test_package_omega_rate_matrix_matches_oracle():
+    """The synthetic-data module's OmegaModel rate matrix (used to simulate the differentiation
+    workload) against the oracle's restatement of src/OmegaModel.ml:21-80, on uniform and skewed
+    F3x4 frequencies and both sigma settings."""
+    from phylocsf_gb300 import synth
+    from oracle import omega as W
+    for q in ([2.5, 0.3, 1.0] + [1.0] * 9, [1.7, 1.4, 0.01, 0.8, 1.2, 1.1, 0.9, 1.0, 1.3, 0.7, 1.5, 1.05]):
+        Q, pi = W.omega_q(q)
+        Q2, pi2 = synth.omega_rate_matrix(q[0], q[1], q[2], np.array(q[3:]))
+        assert np.abs(Q - Q2).max() <= 1e-14 and np.abs(pi - pi2).max() <= 1e-15
