@@ -201,6 +201,13 @@ int pcsf_engine_eigensystem(const pcsf_engine *e, int32_t model, double *U, doub
  * P: [n_t][64][64] row-major FP64.  Per-matrix status in status[n_t]. */
 int pcsf_engine_pt(pcsf_engine *e, int32_t model, int32_t n_t, const double *t, double *P, int32_t *status);
 
+/* P(t) as the tensor-core search forms it (TF32 hi/lo products around the FP32
+ * grid, k_pform_tc), for checking: P: [n_t][64][64] row-major (1 <= n_t <= 320),
+ * status [n_t] (one status for the call) may be NULL.  TF32 tensor-core engines
+ * only.  Replaces nothing in the reference: the search's P(t) has no counterpart
+ * (the reference forms every P(t) by Q.Diag.to_Pt, Q.ml:211-256). */
+int pcsf_engine_pt_search(pcsf_engine *e, int32_t model, int32_t n_t, const double *t, double *P, int32_t *status);
+
 /* ---------------------------------------------------------------- batches */
 
 /* Upload a batch of regions.  Region r is columns [col_offsets[r],

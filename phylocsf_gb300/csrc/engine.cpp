@@ -2494,6 +2494,52 @@ int pcsf_engine_pt(pcsf_engine *e, int32_t model, int32_t n_t, const double *t, 
     return PCSF_OK;
 }
 
+int pcsf_engine_pt_search(pcsf_engine *e, int32_t model, int32_t n_t, const double *t, double *P, int32_t *status)
+{
+    if (!e) return PCSF_EINVAL;
+    if (!e->has_models) return e->fail(PCSF_EINVAL, "this engine has no coding / noncoding models");
+    CK(cudaSetDevice(e->device), "cudaSetDevice");
+    if (!(e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32) || !e->dPfB.p)
+        return e->fail(PCSF_EINVAL, "pcsf_engine_pt_search: this engine forms no tensor-core P(t)");
+    if (model < 0 || model > 1 || n_t <= 0 || n_t > 320 || !t || !P)
+        return e->fail(PCSF_EINVAL, "pcsf_engine_pt_search: bad argument (1 <= n_t <= 320)");
+    for (int i = 0; i < n_t; i++)
+        if (!(t[i] >= 0.0) || !std::isfinite(t[i])) return e->fail(PCSF_EINVAL, "pcsf_engine_pt_search: t[%d] = %g", i, t[i]);
+    DevBuf<double> dt;
+    DevBuf<float> dP;
+    DevBuf<PSet> dps;
+    DevBuf<int32_t> dst;
+    CK(dt.reserve(n_t), "cudaMalloc");
+    CK(dP.reserve((size_t)n_t * K2), "cudaMalloc");
+    CK(dps.reserve(1), "cudaMalloc");
+    CK(dst.reserve(1), "cudaMalloc");
+    PSet ps{model, 0, 1.0};
+    CK(cudaMemcpyAsync(dt.p, t, sizeof(double) * n_t, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemcpyAsync(dps.p, &ps, sizeof ps, cudaMemcpyHostToDevice, e->stream), "H2D");
+    CK(cudaMemsetAsync(dst.p, 0x7f, sizeof(int32_t), e->stream), "memset");
+    CK(cudaMemsetAsync(e->derr.p, 0, sizeof(int), e->stream), "memset");
+    // every matrix written as E^T (all "branches" above leaves): t plays the branch lengths at rho = 1
+    CK(launch_pform_tc(dps.p, 1, dt.p, n_t, n_t, e->dm, e->dPfB.p, dP.p, nullptr, dst.p, e->derr.p, e->stream),
+       "tensor-core P(t) launch");
+    e->stats.kernel_launches += 1;
+    std::vector<float> raw((size_t)n_t * K2);
+    int32_t key = STATUS_NONE;
+    int herr = 0;
+    CK(cudaMemcpyAsync(raw.data(), dP.p, sizeof(float) * raw.size(), cudaMemcpyDeviceToHost, e->stream), "D2H");
+    CK(cudaMemcpyAsync(&key, dst.p, sizeof(int32_t), cudaMemcpyDeviceToHost, e->stream), "D2H");
+    CK(cudaMemcpyAsync(&herr, e->derr.p, sizeof(int), cudaMemcpyDeviceToHost, e->stream), "D2H");
+    CK(cudaStreamSynchronize(e->stream), "P(t)");
+    if (herr) return e->fail(PCSF_ECUDA, "pcsf_engine_pt_search: a tensor-core wait timed out");
+    const int st = (key >= 0 && key < 0x7f000000) ? (key & 15) : PCSF_OK;
+    for (int i = 0; i < n_t; i++) {
+        if (status) status[i] = st;
+        for (int r = 0; r < K; r++)
+            for (int c = 0; c < K; c++)
+                P[(size_t)i * K2 + r * K + c] = (double)raw[(size_t)i * K2 + (size_t)c * K + r] + (r == c ? 1.0 : 0.0);
+    }
+    return PCSF_OK;
+}
+
 int pcsf_batch_create(pcsf_engine *e, int32_t n_regions, const int64_t *col_offsets, const uint8_t *leaves,
                       pcsf_batch **out)
 {

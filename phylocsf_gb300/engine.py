@@ -122,6 +122,7 @@ SIGNATURES = {
     "pcsf_engine_set_exact_threshold": ([_VP, ctypes.c_int64], ctypes.c_int),
     "pcsf_engine_exact_available": ([_VP], ctypes.c_int),
     "pcsf_engine_autotune": ([_VP, _VP, _I32], ctypes.c_int),
+    "pcsf_engine_pt_search": ([_VP, ctypes.c_int32, ctypes.c_int32, _D, _D, _I32], ctypes.c_int),
     "pcsf_branch_counts": ([_VP, _VP, ctypes.c_int32, _D, _D, _D, _I32], ctypes.c_int),
     "pcsf_ell": ([_VP, ctypes.c_int32, ctypes.c_double, _D, _D], ctypes.c_int),
     "pcsf_node_posteriors": ([_VP, _VP, ctypes.c_int32, _D, ctypes.c_int32, _I32, _D, _I32], ctypes.c_int),
@@ -476,6 +477,15 @@ class Engine:
         _check(self.lib.pcsf_engine_pt(self.handle, model, len(tt), _p(tt, ctypes.c_double), _p(P, ctypes.c_double),
                                        _p(st, ctypes.c_int32)), self.handle)
         return P, st
+
+    def pt_search(self, model: int, t) -> Tuple[np.ndarray, np.ndarray]:
+        """P(t) as the tensor-core search forms it (TF32 tensor-core engines)."""
+        tt = np.ascontiguousarray(t, np.float64)
+        P_ = np.zeros((len(tt), 64, 64))
+        st = np.zeros(len(tt), np.int32)
+        _check(self.lib.pcsf_engine_pt_search(self.handle, model, len(tt), _p(tt, ctypes.c_double),
+                                              _p(P_, ctypes.c_double), _p(st, ctypes.c_int32)), self.handle)
+        return P_, st
 
     def eigensystem(self, model: int) -> Tuple[np.ndarray, np.ndarray]:
         U = np.zeros((64, 64))

@@ -3,8 +3,8 @@
 Tolerances: FP64 engine, per-branch d lpr / d t within 1e-7 relative (abs
 floor 1e-8) of the oracle (the oracle differentiates P(t) = exp(tQ)
 analytically, the kernel applies dP/dt = Q P to P after the clamp /
-renormalise row rule); FP32 (compensated) within 1e-3 relative of the
-largest |gradient| entry.  d lpr / d rho against a central difference of the
+renormalise row rule); FP32 (compensated or blocked) per entry within 1e-4
+relative plus 2e-6 per column of the region.  d lpr / d rho against a central difference of the
 FP64 engine's lpr with h = 1e-5: within 1e-6 relative.
 """
 import numpy as np
@@ -18,6 +18,7 @@ from tests import helpers as H
 pytestmark = pytest.mark.gpu
 
 _E = {}
+_G = {}     # oracle gradients, shared by the precisions
 
 
 def engine(name, prec):
@@ -39,12 +40,13 @@ def _fast():
     O.set_sparse_leaves(True)
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
-@pytest.mark.parametrize("name", ["12flies", "29mammals"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32c", "fp32b"])
+@pytest.mark.parametrize("name", ["12flies", "29mammals", "58mammals", "100vertebrates"])
 def test_branch_gradient_matches_oracle(prec, name):
     e = engine(name, prec)
     mc, mn, ot, tree = H.oracle_models(name)
-    offs, leaves = _data(name, [90, 1, 200, 0], seed=21)
+    lengths = [90, 1, 200, 0] if name in ("12flies", "29mammals") else [90, 1, 333, 0, 700, 64]
+    offs, leaves = _data(name, lengths, seed=21)
     b = e.batch(offs, leaves)
     for model, om in ((0, mc), (1, mn)):
         for rho in (0.3, 1.0, 2.5):
@@ -52,7 +54,10 @@ def test_branch_gradient_matches_oracle(prec, name):
             assert (st == 0).all()
             for r in range(len(offs) - 1):
                 lv = H.u8_to_oracle(leaves[offs[r]:offs[r + 1]])
-                lo, go = O.grad_branches(om, ot, rho, lv)
+                key = (name, model, rho, r)
+                if key not in _G:
+                    _G[key] = O.grad_branches(om, ot, rho, lv)
+                lo, go = _G[key]
                 if lv.shape[0] == 0:
                     assert np.all(db[r] == 0.0) and lpr[r] == 0.0
                     continue
@@ -62,8 +67,11 @@ def test_branch_gradient_matches_oracle(prec, name):
                     k = int(np.argmax(err))
                     assert err[k] <= 0, (model, rho, r, k, db[r][k], go[k], tree.branch[k])
                 else:
-                    scale = np.abs(go).max()
-                    assert np.abs(db[r] - go).max() <= 1e-3 * scale + 1e-6, (np.abs(db[r] - go).max(), scale)
+                    # per entry: 1e-4 relative plus 2e-6 per column (the FP32 rounding of each
+                    # column's term), so near-zero entries are held to an absolute bound
+                    err = np.abs(db[r] - go) - (1e-4 * np.abs(go) + 2e-6 * lv.shape[0])
+                    k = int(np.argmax(err))
+                    assert err[k] <= 0, (model, rho, r, k, db[r][k], go[k])
                 assert drho[r] == pytest.approx(float(tree.branch[: tree.n - 1] @ db[r]), rel=1e-12, abs=1e-12)
 
 

@@ -66,13 +66,40 @@ def test_pt_matches_oracle(prec):
             assert (Pg[i] >= 0).all()
 
 
-def test_eigensystem_matches_oracle():
-    e = engine("12flies", "fp64")
-    mc, mn, ot, tree = H.oracle_models("12flies")
+@pytest.mark.parametrize("name", ["12flies", "29mammals", "58mammals", "100vertebrates", "120mammals"])
+def test_eigensystem_matches_oracle(name):
+    """k_jacobi (FP64 cyclic Jacobi on the GPU) against the oracle's Jacobi on the CPU, for both
+    models of every parameter set: eigenvalues within 1e-12, U orthonormal within 1e-12, and
+    D^-1/2 U diag(lam) U^T D^1/2 reproducing Q within 1e-12."""
+    e = engine(name, "fp64")
+    mc, mn, ot, tree = H.oracle_models(name)
     for m, om in ((0, mc), (1, mn)):
         U, lam = e.eigensystem(m)
         assert np.allclose(np.sort(lam), np.sort(om.lam), atol=1e-12)
         assert np.allclose(U.T @ U, np.eye(64), atol=1e-12)
+        sq = np.sqrt(om.pi)
+        Qr = (U * lam) @ U.T * sq[None, :] / sq[:, None]
+        assert np.abs(Qr - om.Q).max() <= 1e-12
+
+
+@pytest.mark.parametrize("name", ["58mammals", "100vertebrates"])
+def test_search_pt_matches_oracle(name):
+    """k_pform_tc, the tensor-core P(t) of the search (TF32 hi/lo products around the FP32 grid),
+    against the oracle's FP64 P(t): entries within 2e-6, rows summing to 1 within 1e-6, no negative
+    entries, over t from 0 to the longest branch at rho = 9.9."""
+    e = engine(name, "tf32x3")
+    mc, mn, ot, tree = H.oracle_models(name)
+    bmax = tree.branch[: tree.n - 1].max()
+    # t = 0, below the FP32 grid (Taylor), on and between grid points, up to rho = 9.9 on the longest branch
+    ts = np.array([0.0, 4e-6, 1e-5, 3e-4, 0.00655, 0.05, 0.3, 1.0, 0.5 * bmax, 3.3 * bmax, 9.9 * bmax])
+    for m, om in ((0, mc), (1, mn)):
+        Pg, st = e.pt_search(m, ts)
+        assert (st == 0).all()
+        for i, t in enumerate(ts):
+            Po = om.pt(t)
+            assert np.abs(Pg[i] - Po).max() <= 2e-6, (m, t, np.abs(Pg[i] - Po).max())
+            assert np.allclose(Pg[i].sum(1), 1.0, atol=1e-6)
+            assert (Pg[i] >= 0).all()
 
 
 def _synthetic(name, lengths, seed, gaps=(0.05, 0.4), missing=0.2):
