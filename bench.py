@@ -364,6 +364,9 @@ def run_ours(args, world, rank, local):
     t_at = time.perf_counter()
     tile = eng.autotune(batch) if not args.no_autotune else None
     autotune_s = time.perf_counter() - t_at
+    tc_shape_ms = None
+    if tile is not None and eng.stats()["tc_shape"] >= 0:
+        tc_shape_ms = {P.Engine.TC_SHAPES[k]: round(float(v), 3) for k, v in enumerate(eng.tc_shape_times())}
 
     # inputs smaller than twice the L2 (129 MB) get an L2 flush before every timed step
     flush = None
@@ -454,8 +457,10 @@ def run_ours(args, world, rank, local):
             "precision": args.precision,
             "launch": {"ctas": {"simt_prune": st["prune_grid"], "tensor_core_prune": st["tc_grid"]},
                        "simt_tile": st["simt_tile"],
+                       "tc_shape": P.Engine.TC_SHAPES.get(st["tc_shape"]),
                        "autotune": None if tile is None else {"chosen_tile": tile, "seconds": autotune_s,
-                                                              "candidates": [64, 32]}},
+                                                              "candidates": [64, 32],
+                                                              "tc_shape_ms": tc_shape_ms}},
             "column_branches_per_s": colb_per_s,
             "e2e": {"value": e2e_value, "unit": "regions/s", "h2d_bytes_per_step": int(wl.leaves.nbytes +
                                                                                        wl.col_offsets.nbytes),

@@ -126,6 +126,7 @@ typedef struct {
     int32_t prune_grid;     /* launch configuration (not counters): CTAs of the SIMT pruning kernel, */
     int32_t tc_grid;        /* and of the tensor-core kernel (0 if the engine has none),             */
     int32_t simt_tile;      /* and the SIMT kernel's column tile                                     */
+    int32_t tc_shape;       /* and the TF32 tensor-core search kernel's shape (-1: none; see below)  */
 } pcsf_stats;
 
 /* ---------------------------------------------------------------- engine */
@@ -184,8 +185,21 @@ int pcsf_engine_exact_available(const pcsf_engine *e);
  * rho = 1, one warm-up and two timed passes each); the fastest is kept for every
  * later call on this engine and written to *tile (may be NULL).  The choice depends
  * on the tree (partial slots and leaves) and the precision.  The FP64 engine has one
- * tile (32) and keeps it.  No reference counterpart (the reference has no device). */
+ * tile (32) and keeps it.  TF32 tensor-core engines also time the search kernel's
+ * shapes on the same sample and keep the faster (pcsf_stats.tc_shape):
+ *   0: each column's partial (alpha) kept in registers from the operand staging to the
+ *      epilogue;  1: alpha read back from the MMA operands in the epilogue.
+ * Both issue the same MMAs on the same operands: the values are identical.
+ * No reference counterpart (the reference has no device). */
 int pcsf_engine_autotune(pcsf_engine *e, pcsf_batch *b, int32_t *tile);
+
+/* Set the TF32 tensor-core search kernel's shape (0 or 1, above) by hand; TF32
+ * tensor-core engines only. */
+int pcsf_engine_set_tc_shape(pcsf_engine *e, int32_t shape);
+
+/* The autotuner's device time per pass of each search-kernel shape (ms; 0 where
+ * untimed), n entries at most. */
+int pcsf_engine_tc_shape_times(const pcsf_engine *e, double *ms, int32_t n);
 
 /* The CUDA stream (a cudaStream_t) on which the engine launches all of its
  * work, so that callers can time it with events on that stream.  No reference

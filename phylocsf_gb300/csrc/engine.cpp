@@ -143,6 +143,8 @@ struct pcsf_engine {
     DevBuf<double> ddpart, ddrho, ddscr;
     bool dual_ok = false;          // the tangent pass fits this tree
     int tc_grid = 0;
+    int tc_shape = 0;              // TF32 tensor-core search kernel's shape (set by pcsf_engine_autotune)
+    double tc_shape_ms[PCSF_TC_SHAPES] = {};   // the autotuner's time per pass of each shape (0: untimed)
     size_t pbuf_psets = 0;
     DevBuf<PSet> dps;
     DevBuf<Request> dreq;
@@ -606,7 +608,8 @@ static int engine_init_common(pcsf_engine *e, const pcsf_tree *tree, int32_t fla
     if (tc && prune_tc_smem_bytes(e->nl, (int)e->sched.size()) > (size_t)prop.sharedMemPerBlockOptin)
         return e->fail(PCSF_EINVAL, "tensor-core path needs %zu B shared memory",
                        prune_tc_smem_bytes(e->nl, (int)e->sched.size()));
-    if (tc) e->tc_grid = prop.multiProcessorCount * prune_tc_ctas_per_sm(e->nslots, e->nl, (int)e->sched.size());
+    if (tc)
+        e->tc_grid = prop.multiProcessorCount * prune_tc_ctas_per_sm(e->nslots, e->nl, (int)e->sched.size(), e->tc_shape);
     size_t smem = prune_smem_bytes(e->prec, e->nslots, e->nl, (int)e->sched.size());
     if (smem > (size_t)prop.sharedMemPerBlockOptin)
         return e->fail(PCSF_EINVAL, "tree needs %d partial slots (%zu B shared memory > %zu)", e->nslots, smem,
@@ -850,6 +853,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
         pa.dither = e->prec != PCSF_PREC_FP64;
         pa.dlo = dlo;
         pa.tile = e->simt_tile;
+        pa.tc_shape = e->tc_shape;
         if (grad) {
             GradArgs ga{};
             ga.wi = pa.wi;
@@ -2356,6 +2360,7 @@ int pcsf_engine_get_stats(const pcsf_engine *e, pcsf_stats *out)
     *out = e->stats;
     out->prune_grid = e->prune_grid;
     out->tc_grid = e->tc_grid;
+    out->tc_shape = (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32) ? e->tc_shape : -1;
     out->simt_tile = simt_tile_cols(e->prec, e->nslots, e->simt_tile);
     return PCSF_OK;
 }
@@ -2415,6 +2420,59 @@ int pcsf_engine_autotune(pcsf_engine *e, pcsf_batch *b, int32_t *tile)
     e->simt_tile = best;
     e->prune_grid = simt_grid(e, best);
     if (tile) *tile = best;
+    // the TF32 search kernel's shape (the values do not depend on it), timed on the same
+    // sample's search evaluations
+    if (e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32) {
+        const int saved_shape = e->tc_shape, saved_tc_grid = e->tc_grid;
+        const pcsf_stats keep = e->stats;
+        int best_s = -1;
+        double best_s_ms = 1e300;
+        for (int cand = 0; cand < PCSF_TC_SHAPES; cand++) {
+            e->tc_shape = cand;
+            e->tc_grid = e->sm_count * prune_tc_ctas_per_sm(e->nslots, e->nl, (int)e->sched.size(), cand);
+            double ms = 0.0;
+            std::vector<Eval> res;
+            for (int it = 0; it < 3 && rc == PCSF_OK; it++) {
+                const double before = e->stats.kind_ms[1];
+                rc = evaluate(e, b, reqs, res, nullptr, false);
+                if (it > 0) ms += e->stats.kind_ms[1] - before;
+            }
+            if (rc != PCSF_OK) break;
+            e->tc_shape_ms[cand] = ms / 2.0;
+            if (ms < best_s_ms) {
+                best_s_ms = ms;
+                best_s = cand;
+            }
+        }
+        e->stats = keep;
+        if (rc != PCSF_OK || best_s < 0) {
+            e->tc_shape = saved_shape;
+            e->tc_grid = saved_tc_grid;
+            return rc != PCSF_OK ? rc : e->fail(PCSF_EINVAL, "pcsf_engine_autotune: no tensor-core shape fits");
+        }
+        e->tc_shape = best_s;
+        e->tc_grid = e->sm_count * prune_tc_ctas_per_sm(e->nslots, e->nl, (int)e->sched.size(), best_s);
+    }
+    return PCSF_OK;
+}
+
+int pcsf_engine_set_tc_shape(pcsf_engine *e, int32_t shape)
+{
+    if (!e) return PCSF_EINVAL;
+    if (!(e->prec == PCSF_PREC_TF32X3 || e->prec == PCSF_PREC_TF32))
+        return e->fail(PCSF_EINVAL, "pcsf_engine_set_tc_shape: this engine has no TF32 tensor-core search kernel");
+    if (!prune_tc_shape_ok(shape))
+        return e->fail(PCSF_EINVAL, "pcsf_engine_set_tc_shape: shape must be 0..%d", PCSF_TC_SHAPES - 1);
+    CK(cudaSetDevice(e->device), "cudaSetDevice");
+    e->tc_shape = shape;
+    e->tc_grid = e->sm_count * prune_tc_ctas_per_sm(e->nslots, e->nl, (int)e->sched.size(), shape);
+    return PCSF_OK;
+}
+
+int pcsf_engine_tc_shape_times(const pcsf_engine *e, double *ms, int32_t n)
+{
+    if (!e || !ms || n < 0) return PCSF_EINVAL;
+    for (int i = 0; i < n && i < PCSF_TC_SHAPES; i++) ms[i] = e->tc_shape_ms[i];
     return PCSF_OK;
 }
 

@@ -116,6 +116,7 @@ struct PruneArgs {
     int dither;              // SIMT FP32 kernel: per-column dithering of the leaf partials (prune_common.cuh)
     const float *dlo;        // SIMT FP32 kernel, may be null: per chunk-local P set [nbr][K] low parts of diag(E)
     int tile;                // SIMT FP32 kernel: column tile 32 or 64, 0 = the default rule (simt_tile_cols)
+    int tc_shape;            // TF32 tensor-core kernel: 0 alpha kept in registers, 1 read back (identical values)
 };
 // comp: 0 plain FP32 sums, 1 Kahan, 2 blocked Kahan (see prune_common.cuh)
 cudaError_t launch_prune(int prec, int comp, const PruneArgs &a, cudaStream_t s, int grid);
@@ -162,7 +163,9 @@ cudaError_t launch_reduce_grad(const double *gpart, const int32_t *wi_begin, int
 cudaError_t launch_prune_tc(int nprod, const PruneArgs &a, int *err, cudaStream_t s, int grid);
 size_t prune_tc_smem_bytes(int nl, int nint);
 bool prune_tc_supported(int nslots, int nl);
-int prune_tc_ctas_per_sm(int nslots, int nl, int nint);
+constexpr int PCSF_TC_SHAPES = 2;
+int prune_tc_ctas_per_sm(int nslots, int nl, int nint, int shape);
+bool prune_tc_shape_ok(int shape);
 // Tensor-core pruning with BF16 split products (tc_bf16.cu): x = h + m + l, six
 // products on tcgen05 kind::f16, FP32 accumulation; E^T of every branch in Pbuf (FP32).
 cudaError_t launch_prune_bf16(const PruneArgs &a, int *err, cudaStream_t s, int grid);

@@ -33,8 +33,9 @@
 // 256-bit loads, and while a node's MMAs run its threads prefetch into L1 the leaf
 // rows of the next node.
 //
-// Shared memory (about 106 KB for 58 leaves): one A operand (128 x 64, hi + lo),
-// one B operand (64 x 64, hi + lo), the tile's leaf states and the schedule.
+// Shared memory (about 106 KB for 58 leaves, 112 KB for 100, so that two CTAs share an
+// SM): one A operand (128 x 64, hi + lo), one B operand (64 x 64, hi + lo), the tile's
+// leaf states and the schedule.
 // The two children of a node are contracted one after the other through the
 // same operand buffers.  B operands are pre-split by the P(t) kernel into this
 // exact layout, so one elected thread fetches each with a single 32 KB bulk copy
@@ -76,7 +77,12 @@ constexpr uint32_t SM_LV = 98304;       // [nl][LV_STRIDE] leaf states, then the
 constexpr uint32_t A_BYTES = 32768, B_BYTES = 16384;
 // leaf-state rows padded by 4 bytes: the tile fill writes one byte per (site, leaf)
 // with consecutive threads on consecutive leaves, which would otherwise all hit one bank
-constexpr int LV_STRIDE = TCP_M + 4;
+constexpr int LV_STRIDE = TCP_M;     // leaf-state rows: [leaf][site] bytes, words XOR-swizzled per row
+// byte offset of (leaf l, site c): row l's 4-byte words are permuted by XOR with l mod 32,
+// so that the fill (consecutive threads on consecutive leaves of one site) and the reads
+// (consecutive threads on consecutive sites of one leaf) are both free of bank conflicts
+// without padding the rows (whose bytes decide whether two CTAs fit an SM on 100 leaves)
+__device__ __forceinline__ int lv_off(int l, int c) { return l * LV_STRIDE + (c ^ ((l & 31) << 2)); }
 
 
 // alpha = hi + lo of this thread's 32 states, read back from the A operand
@@ -94,7 +100,12 @@ __device__ __forceinline__ void load_alpha(const unsigned char *sm, int site, in
     }
 }
 
-template <int NPROD>
+// KEEP: each column's partial (alpha) stays in registers from the operand staging to
+// the epilogue, which then reads only D (else the epilogue reads alpha back from the
+// operands, and the second child's staging waits for a barrier that frees them).  Both
+// shapes issue the same MMAs on the same operands and produce identical values; the
+// engine's autotuner times them.
+template <int NPROD, bool KEEP>
 __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32_t tmem_cols, int *err)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
@@ -102,10 +113,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
     __shared__ __align__(8) uint64_t bar_mma, bar_b;
     __shared__ float cmax[2][2][TCP_M];
     __shared__ double red_l[TCP_THREADS / 32], red_e[TCP_THREADS / 32];
-    __shared__ int16_t bseq[TCP_MAX_LEAVES];     // internal children in contraction order
-    __shared__ int8_t dreg[TCP_MAX_LEAVES];      // per contraction: free region for D, or -1
     __shared__ int nbseq_s;
-    __shared__ float prf[K], wlf[K];             // this work item's model: prior, prior * log prior (FP32)
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int site = tid & (TCP_M - 1);          // tile column = TMEM lane
@@ -114,6 +122,10 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
     const int nl = a.nl;
     uint8_t *lvT = sm + SM_LV;
     SchedNode *sched = reinterpret_cast<SchedNode *>(sm + SM_LV + ((nl * LV_STRIDE + 15) & ~15));
+    // per contraction (fewer than n_internal): the internal child, in order, and the free
+    // tensor-memory region for D or -1
+    int16_t *bseq = reinterpret_cast<int16_t *>(sched + a.n_internal);
+    int8_t *dreg = reinterpret_cast<int8_t *>(bseq + a.n_internal);
     const uint32_t barM = smem_addr(&bar_mma), barB = smem_addr(&bar_b);
     const uint32_t sA = smem_addr(sm + SM_A), sB = smem_addr(sm + SM_B);
     // kind::tf32, D f32, A/B tf32, both K-major, N = 64, M = 128
@@ -173,11 +185,33 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
     if (tid == 0) issue_next_b();
 
     // stage alpha of slot s (this thread's 32 states) as the A operand: lo to shared
-    // memory; hi to shared memory (shared form) or back over slot s (region form)
+    // memory; hi to shared memory (shared form) or back over slot s (region form); with
+    // KEEP, alpha itself stays in al for the epilogue
     // (the output stores of earlier nodes are waited for here, before the first read)
-    auto stage_a = [&](int s, bool region) {
+    auto stage_a = [&](int s, bool region, float *al) {
         const uint32_t ts = tbase + lane_off + 64 * s + s0;
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        if constexpr (KEEP) {
+            tmem_ld16x2(ts, ts + 16, al, al + 16);
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                float h[16];
+#pragma unroll
+                for (int j4 = 0; j4 < 4; j4++) {
+                    const float *y = al + 16 * q + 4 * j4;
+                    const float4 hv = make_float4(tf32_hi(y[0]), tf32_hi(y[1]), tf32_hi(y[2]), tf32_hi(y[3]));
+                    const float4 lv = make_float4(y[0] - hv.x, y[1] - hv.y, y[2] - hv.z, y[3] - hv.w);
+                    const uint32_t o = core_off(site, s0 + 16 * q + 4 * j4, 16);
+                    if (!region) *reinterpret_cast<float4 *>(sm + SM_A + o) = hv;
+                    *reinterpret_cast<float4 *>(sm + SM_A + A_BYTES + o) = lv;
+                    h[4 * j4] = hv.x; h[4 * j4 + 1] = hv.y; h[4 * j4 + 2] = hv.z; h[4 * j4 + 3] = hv.w;
+                }
+                if (region) tmem_st16(ts + 16 * q, h);
+            }
+            if (region) asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            return;
+        }
         float x[32];
         tmem_ld16x2(ts, ts + 16, x, x + 16);
 #pragma unroll
@@ -238,15 +272,19 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                      :: "r"(barM) : "memory");
     };
-    // v (or v *=) alpha + D for the internal child in slot s, alpha = hi + lo from
-    // where stage_a put them
-    auto child_value = [&](int s, int r, float *v, bool mul) {
+    // v (or v *=) alpha + D for the internal child in slot s, alpha from the registers
+    // the staging filled (KEEP) or hi + lo from where the staging put them
+    auto child_value = [&](int s, int r, const float *al, float *v, bool mul) {
         const uint32_t tD = tbase + lane_off + 64 * (r >= 0 ? r : s) + s0;
         const uint32_t tH = tbase + lane_off + 64 * s + s0;
 #pragma unroll
         for (int q = 0; q < 2; q++) {
             float d[16], x[16];
-            if (r >= 0) {
+            if constexpr (KEEP) {
+                tmem_ld16(tD + 16 * q, d);
+#pragma unroll
+                for (int j = 0; j < 16; j++) x[j] = al[16 * q + j];
+            } else if (r >= 0) {
                 tmem_ld16x2(tD + 16 * q, tH + 16 * q, d, x);
 #pragma unroll
                 for (int j4 = 0; j4 < 4; j4++) {
@@ -304,11 +342,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
         __syncthreads();
         for (int f = tid; f < TCP_M * nl; f += TCP_THREADS) {
             int c = f / nl, l = f - c * nl;
-            lvT[l * LV_STRIDE + c] = (c < ncols) ? lg[f] : (uint8_t)K;
-        }
-        if (tid < K) {
-            prf[tid] = (float)a.m.prior[md * K + tid];
-            wlf[tid] = (float)a.m.wlog[md * K + tid];
+            lvT[lv_off(l, c)] = (c < ncols) ? lg[f] : (uint8_t)K;
         }
         __syncthreads();
         // warm L1 with the leaf rows (one 128-byte line per thread and leaf) of the node
@@ -317,11 +351,11 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
             if (ni + 1 >= a.n_internal) return;
             const SchedNode nx = sched[ni + 1];
             if (nx.lslot < 0) {
-                const int sa = lvT[nx.lc * LV_STRIDE + site];
+                const int sa = lvT[lv_off(nx.lc, site)];
                 asm volatile("prefetch.global.L1 [%0];" :: "l"(Pbase + (size_t)nx.lc * K2 + (size_t)(sa < K ? sa : 0) * K + s0));
             }
             if (nx.rslot < 0) {
-                const int sb = lvT[nx.rc * LV_STRIDE + site];
+                const int sb = lvT[lv_off(nx.rc, site)];
                 asm volatile("prefetch.global.L1 [%0];" :: "l"(Pbase + (size_t)nx.rc * K2 + (size_t)(sb < K ? sb : 0) * K + s0));
             }
         };
@@ -342,7 +376,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
             // warp 0 (whose thread 0 issues the MMAs) loads its leaf rows before the staging
             int ls0 = K;
             if (nint == 1 && warp == 0) {
-                ls0 = lvT[lfc * LV_STRIDE + site];
+                ls0 = lvT[lv_off(lfc, site)];
                 leaf_load(Pbase + (size_t)lfc * K2, ls0, v);
             }
             bool have = (nint == 1), bad = false;
@@ -350,9 +384,13 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
             for (int side = 0; side < 2; side++) {
                 const int s = side ? slotR : slotL;
                 if (s < 0) continue;
-                if (nc++ && __syncthreads_or(bad)) { ok = false; break; }   // the A operand is free again
+                // the A operand is free again (with KEEP it is once the MMAs have completed,
+                // and the first child's D is read before the staging barrier below)
+                if (!KEEP && nc && __syncthreads_or(bad)) { ok = false; break; }
+                nc++;
                 const int r = dreg[kc++];
-                stage_a(s, r >= 0);
+                float al[KEEP ? 32 : 1];
+                stage_a(s, r >= 0, al);
                 if (tid == 0 && !wait_b()) bad = true;
                 tc_fence_before();
                 if (__syncthreads_or(bad)) { ok = false; break; }
@@ -361,7 +399,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
                 prefetch_next(ni);      // while the MMAs run
                 if (nint == 1) {
                     if (warp != 0) {
-                        ls0 = lvT[lfc * LV_STRIDE + site];
+                        ls0 = lvT[lv_off(lfc, site)];
                         leaf_load(Pbase + (size_t)lfc * K2, ls0, v);
                     }
                     leaf_fix(ls0, v);
@@ -371,13 +409,13 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
                 if (!done) bad = true;
                 else ph_mma ^= 1u;   // after a timed-out wait the quiesce waits for this phase
                 if (tid == 0 && done) issue_next_b();     // the B operand is free again
-                child_value(s, r, v, have);
+                child_value(s, r, al, v, have);
                 have = true;
             }
             if (!ok) break;
             if (nint == 0) {
-                leaf_value(Pbase + (size_t)sn.lc * K2, lvT[sn.lc * LV_STRIDE + site], v, false);
-                leaf_value(Pbase + (size_t)sn.rc * K2, lvT[sn.rc * LV_STRIDE + site], v, true);
+                leaf_value(Pbase + (size_t)sn.lc * K2, lvT[lv_off(sn.lc, site)], v, false);
+                leaf_value(Pbase + (size_t)sn.rc * K2, lvT[lv_off(sn.rc, site)], v, true);
             }
             // ---- rescale by an exact power of two and park in the output slot
             float mx = 0.0f;
@@ -403,7 +441,14 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
         // log z = log m + e ln 2 with m in [0.5, 1) (logf of m is within ~4e-8 absolute,
         // far below the tensor-core noise of these search values); FP64 only for the
         // per-column log and the sums over the tile (this part's FP64 rate is ~1/64 of FP32)
-        float *zpart = reinterpret_cast<float *>(sm + SM_A);   // [2][2][128]; the A operand is idle here
+        // (the A operand is idle here: [2][2][128] partial sums, then the model's prior and
+        // prior * log prior in FP32)
+        float *zpart = reinterpret_cast<float *>(sm + SM_A);
+        float *prf = zpart + 4 * TCP_M, *wlf = prf + K;
+        if (tid < K) {
+            prf[tid] = (float)a.m.prior[md * K + tid];
+            wlf[tid] = (float)a.m.wlog[md * K + tid];
+        }
         __syncthreads();
         {
             const uint32_t tR = tbase + lane_off + 64 * sched[a.n_internal - 1].oslot + s0;
@@ -485,60 +530,74 @@ static uint32_t tmem_cols_for(int nslots)
 
 size_t prune_tc_smem_bytes(int nl, int nint)
 {
-    return SM_LV + (((size_t)nl * LV_STRIDE + 15) & ~(size_t)15) + (size_t)nint * sizeof(SchedNode);
+    // operands, leaf states, the schedule, then per contraction the child and the D region
+    return SM_LV + (((size_t)nl * LV_STRIDE + 15) & ~(size_t)15) + (size_t)nint * (sizeof(SchedNode) + 3);
 }
 
 bool prune_tc_supported(int nslots, int nl) { return nslots <= TCP_MAX_SLOTS && nl <= TCP_MAX_LEAVES; }
 
-template <int NPROD>
+bool prune_tc_shape_ok(int shape) { return shape >= 0 && shape < PCSF_TC_SHAPES; }
+
+template <int NPROD, bool KEEP>
 static cudaError_t set_tc_attributes(size_t smem)
 {
-    // the whole unified L1 as shared memory, so that two CTAs of ~110 KB fit
-    cudaError_t e = cudaFuncSetAttribute(k_prune_tc<NPROD>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    // the whole unified L1 as shared memory, so that two CTAs of ~115 KB fit
+    cudaError_t e = cudaFuncSetAttribute(k_prune_tc<NPROD, KEEP>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                          (int)cudaSharedmemCarveoutMaxShared);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_prune_tc<NPROD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(k_prune_tc<NPROD, KEEP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     return e;
 }
 
 // CTAs per SM: the smaller of what shared memory and registers allow (from the
 // kernel's attributes and the device limits) and what tensor memory allows
-int prune_tc_ctas_per_sm(int nslots, int nl, int nint)
+template <bool KEEP>
+static int ctas_per_sm(int nslots, int nl, int nint)
 {
     const uint32_t cols = tmem_cols_for(nslots);
     const int by_tmem = (int)(512 / cols);
     const size_t smem = prune_tc_smem_bytes(nl, nint);
-    cudaFuncAttributes fa;
+    cudaFuncAttributes fa, fa1;
     int dev = 0, smem_sm = 0, regs_sm = 0, reserved = 0;
-    if (set_tc_attributes<3>(smem) != cudaSuccess || set_tc_attributes<1>(smem) != cudaSuccess ||
-        cudaFuncGetAttributes(&fa, k_prune_tc<3>) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+    if (set_tc_attributes<3, KEEP>(smem) != cudaSuccess || set_tc_attributes<1, KEEP>(smem) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, k_prune_tc<3, KEEP>) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa1, k_prune_tc<1, KEEP>) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess)
         return 1;
-    const int by_smem = (int)((size_t)smem_sm / (fa.sharedSizeBytes + smem + (size_t)reserved));
-    const int by_regs = regs_sm / (fa.numRegs * TCP_THREADS);
+    const size_t stat = fa.sharedSizeBytes > fa1.sharedSizeBytes ? fa.sharedSizeBytes : fa1.sharedSizeBytes;
+    const int regs = fa.numRegs > fa1.numRegs ? fa.numRegs : fa1.numRegs;
+    const int by_smem = (int)((size_t)smem_sm / (stat + smem + (size_t)reserved));
+    const int by_regs = regs_sm / (regs * TCP_THREADS);
     int n = by_tmem;
     if (by_smem < n) n = by_smem;
     if (by_regs < n) n = by_regs;
     return n > 0 ? n : 1;
 }
 
+// shapes: 0 = alpha kept in registers, 1 = alpha read back from the operands
+int prune_tc_ctas_per_sm(int nslots, int nl, int nint, int shape)
+{
+    return shape == 1 ? ctas_per_sm<false>(nslots, nl, nint) : ctas_per_sm<true>(nslots, nl, nint);
+}
+
+template <int NPROD, bool KEEP>
+static cudaError_t launch_tc(const PruneArgs &a, int *err, cudaStream_t s, int grid)
+{
+    const size_t smem = prune_tc_smem_bytes(a.nl, a.n_internal);
+    cudaError_t e = set_tc_attributes<NPROD, KEEP>(smem);
+    if (e != cudaSuccess) return e;
+    k_prune_tc<NPROD, KEEP><<<grid, TCP_THREADS, smem, s>>>(a, tmem_cols_for(a.nslots), err);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_prune_tc(int nprod, const PruneArgs &a, int *err, cudaStream_t s, int grid)
 {
     if (a.nwi <= 0) return cudaSuccess;
-    const size_t smem = prune_tc_smem_bytes(a.nl, a.n_internal);
-    const uint32_t cols = tmem_cols_for(a.nslots);
-    if (nprod == 3) {
-        cudaError_t e = set_tc_attributes<3>(smem);
-        if (e != cudaSuccess) return e;
-        k_prune_tc<3><<<grid, TCP_THREADS, smem, s>>>(a, cols, err);
-    } else {
-        cudaError_t e = set_tc_attributes<1>(smem);
-        if (e != cudaSuccess) return e;
-        k_prune_tc<1><<<grid, TCP_THREADS, smem, s>>>(a, cols, err);
-    }
-    return cudaGetLastError();
+    const bool keep = a.tc_shape != 1;
+    if (nprod == 3) return keep ? launch_tc<3, true>(a, err, s, grid) : launch_tc<3, false>(a, err, s, grid);
+    return keep ? launch_tc<1, true>(a, err, s, grid) : launch_tc<1, false>(a, err, s, grid);
 }
 
 }  // namespace pcsf

@@ -82,7 +82,8 @@ class Stats(ctypes.Structure):
                 ("prune_launches", ctypes.c_int64), ("pform_launches", ctypes.c_int64),
                 ("kind_launches", ctypes.c_int64 * 5), ("kind_columns", ctypes.c_int64 * 5),
                 ("kind_ms", ctypes.c_double * 5),
-                ("prune_grid", ctypes.c_int32), ("tc_grid", ctypes.c_int32), ("simt_tile", ctypes.c_int32)]
+                ("prune_grid", ctypes.c_int32), ("tc_grid", ctypes.c_int32), ("simt_tile", ctypes.c_int32),
+                ("tc_shape", ctypes.c_int32)]
 
 
 # Every entry point declared in include/*.h, with its ctypes signature.
@@ -122,6 +123,8 @@ SIGNATURES = {
     "pcsf_engine_set_exact_threshold": ([_VP, ctypes.c_int64], ctypes.c_int),
     "pcsf_engine_exact_available": ([_VP], ctypes.c_int),
     "pcsf_engine_autotune": ([_VP, _VP, _I32], ctypes.c_int),
+    "pcsf_engine_set_tc_shape": ([_VP, ctypes.c_int32], ctypes.c_int),
+    "pcsf_engine_tc_shape_times": ([_VP, _D, ctypes.c_int32], ctypes.c_int),
     "pcsf_engine_pt_search": ([_VP, ctypes.c_int32, ctypes.c_int32, _D, _D, _I32], ctypes.c_int),
     "pcsf_branch_counts": ([_VP, _VP, ctypes.c_int32, _D, _D, _D, _I32], ctypes.c_int),
     "pcsf_ell": ([_VP, ctypes.c_int32, ctypes.c_double, _D, _D], ctypes.c_int),
@@ -478,6 +481,18 @@ class Engine:
                                        _p(st, ctypes.c_int32)), self.handle)
         return P, st
 
+    TC_SHAPES = {0: "alpha kept in registers", 1: "alpha read back"}
+
+    def set_tc_shape(self, shape: int) -> None:
+        """Shape of the TF32 tensor-core search kernel (TC_SHAPES; identical values)."""
+        _check(self.lib.pcsf_engine_set_tc_shape(self.handle, shape), self.handle)
+
+    def tc_shape_times(self) -> np.ndarray:
+        """The autotuner's ms per pass of each search-kernel shape (0 where untimed)."""
+        out = np.zeros(len(self.TC_SHAPES))
+        _check(self.lib.pcsf_engine_tc_shape_times(self.handle, _p(out, ctypes.c_double), len(out)), self.handle)
+        return out
+
     def pt_search(self, model: int, t) -> Tuple[np.ndarray, np.ndarray]:
         """P(t) as the tensor-core search forms it (TF32 tensor-core engines)."""
         tt = np.ascontiguousarray(t, np.float64)
@@ -518,8 +533,9 @@ class Engine:
         _check(self.lib.pcsf_engine_set_exact_threshold(self.handle, int(units)), self.handle)
 
     def autotune(self, batch: Batch) -> int:
-        """Time the compensated FP32 kernel's column tiles on a sample of the batch, keep the
-        fastest for this engine; returns the chosen tile."""
+        """Time the compensated FP32 kernel's column tiles (and, on TF32 tensor-core engines,
+        the search kernel's shapes) on a sample of the batch, keep the fastest for this
+        engine; returns the chosen tile."""
         t = ctypes.c_int32()
         _check(self.lib.pcsf_engine_autotune(self.handle, batch.handle, ctypes.byref(t)), self.handle)
         return t.value

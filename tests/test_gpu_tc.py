@@ -188,3 +188,44 @@ def test_tangent_pass_matches_adjoint(name, lengths):
             tol = 1e-4 * np.abs(dr64) + 2e-6 * ncols
             assert np.all(np.abs(dr - dr64) <= tol), (model, rho, dr - dr64, tol)
             assert np.all(np.abs(lpr - lpr64) <= 2e-6 * np.abs(lpr64) + 1e-9), (model, rho, lpr - lpr64)
+
+
+@pytest.mark.parametrize("name,lengths", [("12flies", [300, 1, 127, 128, 129, 0, 7]),
+                                          ("29mammals", [200, 129, 5]),
+                                          ("58mammals", [50, 333, 1000]),
+                                          ("100vertebrates", [700, 64, 129]),
+                                          ("120mammals", [150, 64])])
+@pytest.mark.parametrize("prec", ["tf32x3_direct", "tf32_direct"])
+def test_search_kernel_shapes_identical(name, lengths, prec):
+    """The search kernel's shapes (alpha kept in registers or read back from the operands)
+    issue the same MMAs on the same operands: their lpr and elpr are bit-identical, for both
+    models over rho from 0.05 to 9."""
+    ps = synth.load_params(name)
+    e = P.Engine(ps.tree, ps.S_c, ps.pi_c, ps.S_n, ps.pi_n, precision=prec)
+    offs, leaves = _data(name, lengths, seed=17)
+    b = e.batch(offs, leaves)
+    out = {}
+    for shape in P.Engine.TC_SHAPES:
+        e.set_tc_shape(shape)
+        assert e.stats()["tc_shape"] == shape
+        out[shape] = [e.lpr(b, m, rho) for m in (0, 1) for rho in (0.05, 1.0, 9.0)]
+    for shape in P.Engine.TC_SHAPES:
+        for x, y in zip(out[0], out[shape]):
+            assert x[0].tobytes() == y[0].tobytes() and x[1].tobytes() == y[1].tobytes(), shape
+            assert (y[2] == 0).all()
+
+
+def test_mle_same_scores_whatever_the_search_shape():
+    """tf32x3b mle scores: identical whichever shape the search kernel runs in, and the
+    autotuner times every shape and keeps one of them."""
+    ps = synth.load_params("58mammals")
+    e = P.Engine(ps.tree, ps.S_c, ps.pi_c, ps.S_n, ps.pi_n, precision="tf32x3b")
+    offs, leaves = _data("58mammals", [500, 70, 1200, 3, 260], seed=4)
+    res = []
+    for shape in P.Engine.TC_SHAPES:
+        e.set_tc_shape(shape)
+        res.append(e.score_batch(offs, leaves, P.MLE).tobytes())
+    assert all(r == res[0] for r in res)
+    e.autotune(e.batch(offs, leaves))
+    assert e.stats()["tc_shape"] in P.Engine.TC_SHAPES
+    assert (e.tc_shape_times() > 0).all()
