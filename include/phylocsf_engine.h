@@ -232,6 +232,7 @@ int pcsf_engine_pt_search(pcsf_engine *e, int32_t model, int32_t n_t, const doub
  * call with PCSF_EINVAL, naming the first bad column and leaf. */
 int pcsf_batch_create(pcsf_engine *e, int32_t n_regions, const int64_t *col_offsets, const uint8_t *leaves,
                       pcsf_batch **out);
+/* Frees the batch's device memory; valid before or after its engine is destroyed. */
 void pcsf_batch_destroy(pcsf_batch *b);
 
 /* Score every region of a resident batch (PhyloCSFModel.score,

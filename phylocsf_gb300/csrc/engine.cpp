@@ -208,6 +208,7 @@ static inline bool tc_prec(int prec)
 
 struct pcsf_batch {
     pcsf_engine *e = nullptr;
+    int device = 0;       // the engine's device, for destroying the batch after its engine
     int nreg = 0;
     std::vector<int64_t> offs;
     int64_t total_cols = 0;
@@ -2609,6 +2610,7 @@ int pcsf_batch_create(pcsf_engine *e, int32_t n_regions, const int64_t *col_offs
     pcsf_batch *b = new (std::nothrow) pcsf_batch();
     if (!b) return e->fail(PCSF_ENOMEM, "out of host memory");
     b->e = e;
+    b->device = e->device;
     b->nreg = n_regions;
     b->offs.assign(n_regions + 1, 0);
     if (n_regions > 0) {
@@ -2659,7 +2661,8 @@ int pcsf_batch_create(pcsf_engine *e, int32_t n_regions, const int64_t *col_offs
 
 void pcsf_batch_destroy(pcsf_batch *b)
 {
-    if (b && b->e) cudaSetDevice(b->e->device);
+    // the engine may already be destroyed: only the batch's own fields are read
+    if (b) cudaSetDevice(b->device);
     delete b;
 }
 

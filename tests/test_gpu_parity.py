@@ -323,3 +323,19 @@ def test_autotune_keeps_values(name, prec):
     for x, y in zip(before, after):
         np.testing.assert_allclose(y, x, rtol=1e-12, atol=0)
     e.close()
+
+
+def test_batch_outlives_engine():
+    """A batch destroyed after its engine (an explicit close of the engine while batches are
+    still referenced): the batch's destroy reads only its own fields, and calls through a closed
+    engine fail with an error instead of touching freed memory."""
+    ps = synth.load_params("12flies")
+    e = P.Engine(ps.tree, ps.S_c, ps.pi_c, ps.S_n, ps.pi_n, precision="fp32b")
+    offs, leaves = _synthetic("12flies", [40, 7], seed=2)
+    batches = [e.batch(offs, leaves) for _ in range(3)]
+    assert np.isfinite(e.lpr(batches[0], 0, 1.0)[0]).all()
+    e.close()
+    with pytest.raises(P.EngineError):
+        e.lpr(batches[1], 0, 1.0)
+    for b in batches:
+        b.close()
