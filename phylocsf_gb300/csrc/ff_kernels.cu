@@ -17,7 +17,8 @@
 //   - an internal child's v = alpha + sum_j E[a][j] alpha[j] (PhyloLik.ml:89-92)
 //     is a compensated dot product: each hi x hi product is split exactly
 //     (TwoProduct by FMA), its hi part is added with TwoSum, and the product
-//     errors, the TwoSum errors and the hi x lo cross terms are summed in the lo word;
+//     errors with the TwoSum errors, and the two hi x lo cross terms, are summed in
+//     three separate low accumulators (short dependency chains), added at the end;
 //   - node products alpha = v_l * v_r are float-float products;
 //   - each column is rescaled by an exact power of two after every node;
 //   - the root dot with the prior, the log and the tile sums are FP64.
@@ -36,7 +37,7 @@ namespace pcsf {
 namespace {
 
 constexpr int FF_THREADS = 256;
-constexpr int FF_TC = 32;            // columns per tile (2 per thread)
+constexpr int FF_TC = 16;            // columns per tile (1 per thread): ~98 KB of shared memory, two CTAs per SM
 constexpr int FF_CPT = FF_TC / 16;
 
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
@@ -167,19 +168,25 @@ __global__ void __launch_bounds__(FF_THREADS) k_prune_ff(PruneArgs a)
                     // internal: v = alpha + sum_j E[a][j] alpha[j], compensated
                     const float *Eh = Et + side * 2 * K2, *El = Eh + K2;
                     const float *xH = slH + (size_t)slot * K * FF_TC, *xL = slL + (size_t)slot * K * FF_TC;
-                    float sh[4][FF_CPT], sl[4][FF_CPT];
+                    float sh[4][FF_CPT], sa[4][FF_CPT], sb[4][FF_CPT], se[4][FF_CPT];
 #pragma unroll
                     for (int i = 0; i < 4; i++)
 #pragma unroll
-                        for (int cc = 0; cc < FF_CPT; cc++) sh[i][cc] = sl[i][cc] = 0.f;
+                        for (int cc = 0; cc < FF_CPT; cc++) sh[i][cc] = sa[i][cc] = sb[i][cc] = se[i][cc] = 0.f;
 #pragma unroll 2
                     for (int j = 0; j < K; j++) {
                         const float4 eh = *reinterpret_cast<const float4 *>(Eh + j * K + a0);
                         const float4 el = *reinterpret_cast<const float4 *>(El + j * K + a0);
-                        const float2 xh = *reinterpret_cast<const float2 *>(xH + j * FF_TC + c0);
-                        const float2 xl = *reinterpret_cast<const float2 *>(xL + j * FF_TC + c0);
+                        float xhv[FF_CPT], xlv[FF_CPT];
+                        if constexpr (FF_CPT == 2) {
+                            const float2 xh = *reinterpret_cast<const float2 *>(xH + j * FF_TC + c0);
+                            const float2 xl = *reinterpret_cast<const float2 *>(xL + j * FF_TC + c0);
+                            xhv[0] = xh.x; xhv[FF_CPT - 1] = xh.y; xlv[0] = xl.x; xlv[FF_CPT - 1] = xl.y;
+                        } else {
+                            xhv[0] = xH[j * FF_TC + c0];
+                            xlv[0] = xL[j * FF_TC + c0];
+                        }
                         const float ehv[4] = {eh.x, eh.y, eh.z, eh.w}, elv[4] = {el.x, el.y, el.z, el.w};
-                        const float xhv[2] = {xh.x, xh.y}, xlv[2] = {xl.x, xl.y};
 #pragma unroll
                         for (int i = 0; i < 4; i++)
 #pragma unroll
@@ -189,9 +196,9 @@ __global__ void __launch_bounds__(FF_THREADS) k_prune_ff(PruneArgs a)
                                 float s, e;
                                 two_sum(sh[i][cc], p, s, e);
                                 sh[i][cc] = s;
-                                float t = fmaf(ehv[i], xlv[cc], sl[i][cc]);
-                                t = fmaf(elv[i], xhv[cc], t);
-                                sl[i][cc] = t + (pe + e);
+                                sa[i][cc] = fmaf(ehv[i], xlv[cc], sa[i][cc]);
+                                sb[i][cc] = fmaf(elv[i], xhv[cc], sb[i][cc]);
+                                se[i][cc] = se[i][cc] + (pe + e);
                             }
                     }
 #pragma unroll
@@ -201,7 +208,7 @@ __global__ void __launch_bounds__(FF_THREADS) k_prune_ff(PruneArgs a)
                             const float ah = xH[(a0 + i) * FF_TC + c0 + cc], al = xL[(a0 + i) * FF_TC + c0 + cc];
                             float s, e;
                             two_sum(ah, sh[i][cc], s, e);
-                            const float lo = __fadd_rn(__fadd_rn(al, sl[i][cc]), e);
+                            const float lo = __fadd_rn(__fadd_rn(al, (sa[i][cc] + sb[i][cc]) + se[i][cc]), e);
                             fast_two_sum(s, lo, vh[side][i][cc], vl[side][i][cc]);
                         }
                 }

@@ -61,6 +61,9 @@ template <typename T, int CPT> struct ColStore;
 template <> struct ColStore<float, 4> {
     static __device__ inline void store(float *p, const float v[4]) { *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]); }
 };
+template <> struct ColStore<float, 1> {
+    static __device__ inline void store(float *p, const float v[1]) { *p = v[0]; }
+};
 template <> struct ColStore<float, 2> {
     static __device__ inline void store(float *p, const float v[2]) { *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]); }
 };
