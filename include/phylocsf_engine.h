@@ -193,6 +193,15 @@ int pcsf_engine_exact_available(const pcsf_engine *e);
  * No reference counterpart (the reference has no device). */
 int pcsf_engine_autotune(pcsf_engine *e, pcsf_batch *b, int32_t *tile);
 
+/* Adjoint memory (pcsf_grad, pcsf_omega_grad and the derivative rule of engines without
+ * the tangent pass): with on != 0 the outside pass recomputes the partials of leaf
+ * children (one gathered row of P each) instead of storing them, a third less scratch
+ * per CTA for ~5 % more adjoint time; the gradients are identical either way.  Default
+ * off.  pcsf_engine_grad_scratch_bytes gives the scratch per CTA under the current
+ * setting (n_rate_params 0, or 2 for pcsf_omega_grad), -1 on a bad argument. */
+int pcsf_engine_set_grad_recompute(pcsf_engine *e, int32_t on);
+int64_t pcsf_engine_grad_scratch_bytes(const pcsf_engine *e, int32_t n_rate_params);
+
 /* Set the TF32 tensor-core search kernel's shape (0 or 1, above) by hand; TF32
  * tensor-core engines only. */
 int pcsf_engine_set_tc_shape(pcsf_engine *e, int32_t shape);

@@ -153,6 +153,7 @@ struct pcsf_engine {
     DevBuf<double> dpart, dlpr, delpr;
     // gradient path
     DevBuf<unsigned char> gscratch;
+    bool grad_recompute = false;   // adjoint: recompute leaf children's partials instead of storing them
     DevBuf<double> dgpart, dgrad;
     DevBuf<float> dQrowf;
     DevBuf<double> dQrowd;
@@ -785,7 +786,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
     float *bop = want_bop ? e->Bop.p : nullptr;
     size_t gscr = 0;
     if (grad) {
-        gscr = grad_scratch_per_cta(e->prec, e->nl, npar);
+        gscr = grad_scratch_per_cta(e->prec, e->nl, npar, e->grad_recompute);
         CK(e->gscratch.reserve(gscr * (size_t)e->grad_grid), "cudaMalloc gradient scratch");
         CK(e->dgpart.reserve((size_t)std::max(nwi, 1) * gstride), "cudaMalloc");
         CK(e->dgrad.reserve((size_t)nreq * gstride), "cudaMalloc");
@@ -877,6 +878,7 @@ static int evaluate(pcsf_engine *e, pcsf_batch *b, const std::vector<Request> &r
                                 e->dHmat.p, s), "derivative matrix launch");
             ga.scratch = e->gscratch.p;
             ga.scratch_per_cta = gscr;
+            ga.recompute_leaves = e->grad_recompute ? 1 : 0;
             ga.partials = pa.partials;
             ga.gpart = e->dgpart.p + (size_t)wib[r0] * gstride;
             int grid = std::min(e->grad_grid, std::max(pa.nwi, 1));
@@ -2475,6 +2477,20 @@ int pcsf_engine_tc_shape_times(const pcsf_engine *e, double *ms, int32_t n)
     if (!e || !ms || n < 0) return PCSF_EINVAL;
     for (int i = 0; i < n && i < PCSF_TC_SHAPES; i++) ms[i] = e->tc_shape_ms[i];
     return PCSF_OK;
+}
+
+int pcsf_engine_set_grad_recompute(pcsf_engine *e, int32_t on)
+{
+    if (!e) return PCSF_EINVAL;
+    e->grad_recompute = on != 0;
+    return PCSF_OK;
+}
+
+int64_t pcsf_engine_grad_scratch_bytes(const pcsf_engine *e, int32_t n_rate_params)
+{
+    if (!e || (n_rate_params != 0 && n_rate_params != 2)) return -1;
+    return (int64_t)grad_scratch_per_cta(e->prec == PCSF_PREC_FP64 ? PCSF_PREC_FP64 : PCSF_PREC_FP32, e->nl,
+                                         n_rate_params, e->grad_recompute);
 }
 
 int pcsf_engine_set_exact_threshold(pcsf_engine *e, int64_t units)

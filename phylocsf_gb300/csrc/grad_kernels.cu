@@ -11,9 +11,13 @@
 //   inter_c = beta_p . v_s,   d log z / d t_c = inter_c^T Q v_c / z,   beta_c = P_c^T inter_c.
 //
 // One CTA (256 threads) owns a tile of TC columns.  The inside pass is the one of
-// k_prune but also stores every child partial v_c and the per-column exponents
-// of the power-of-two rescaling in a per-CTA global scratch area; the outside
-// pass then walks the schedule in reverse.  Exponent bookkeeping per column:
+// k_prune but also stores the partial v_c of every internal child and the per-column
+// exponents of the power-of-two rescaling in a per-CTA global scratch area; the
+// outside pass then walks the schedule in reverse.  A leaf child's partial is one
+// gathered row of E^T plus the identity (P_c[a][s]); with RECOMP the outside pass
+// recomputes it from the leaf state instead of storing it (the scratch then holds
+// nl - 1 partials and nl - 1 betas instead of 2 nl - 2 and nl - 1: a third less, the
+// same values, ~5 % more time for the scattered re-reads of E^T rows).  Exponent bookkeeping per column:
 // alpha_i = alpha~_i 2^{e(i)} with e(i) = e(l) + e(r) + s_i, beta_c = beta~_c 2^{f(c)}
 // with f(c) = f(p) + e(s) + t_c, and the gradient term carries
 // 2^{f(p) + e(s) + e(c) - e(root)} against the scaled z~.
@@ -26,7 +30,7 @@ namespace pcsf {
 
 constexpr int GR_THREADS = 256;
 
-template <typename T, int TC>
+template <typename T, int TC, bool RECOMP>
 struct GradLayout {
     __host__ __device__ static size_t base(int nslots, int nl, int nint)
     {
@@ -47,10 +51,12 @@ struct GradLayout {
         return sizeof(T) * ((size_t)K2 + (nslots >= 2 ? 0 : 2 * (size_t)K * TC));
     }
     static size_t smem(int nslots, int nl, int nint, int npar) { return base(nslots, nl, nint) + extra(nslots, npar); }
+    // stored child partials: every child's (n - 1), or with RECOMP the internal children's
+    __host__ __device__ static size_t nv(int nl) { return RECOMP ? (size_t)(nl - 1) : (size_t)(2 * nl - 2); }
     static size_t scratch(int nl, int npar)
     {
         const int n = 2 * nl - 1;
-        size_t b = sizeof(T) * ((size_t)(n - 1) + (nl - 1)) * K * TC;
+        size_t b = sizeof(T) * (nv(nl) + (nl - 1)) * K * TC;        // child partials, betas
         b += sizeof(int) * 2 * (size_t)n * TC;
         b = (b + 255) & ~size_t(255);
         if (npar) b += (sizeof(T) * (size_t)(nl - 1) * K * TC + 255) & ~size_t(255);   // alpha of internal nodes
@@ -58,9 +64,10 @@ struct GradLayout {
     }
 };
 
-template <typename T, int TC, int KAHAN>
+template <typename T, int TC, int KAHAN, bool RECOMP>
 __global__ void __launch_bounds__(GR_THREADS) k_grad(GradArgs a)
 {
+    typedef GradLayout<T, TC, RECOMP> Layout;
     constexpr int CPT = TC / 16;
     typedef typename AtomMax<T>::U MU;
     extern __shared__ __align__(16) unsigned char gsm[];
@@ -78,7 +85,7 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad(GradArgs a)
     // parameter derivatives (outside pass only): U and the eigenbasis images of inter and
     // alpha_c over the slots (continuing past them into the extra space at the end of the
     // layout when the slots are fewer), H_x^T in Mat[1]
-    T *Ubuf = reinterpret_cast<T *>(gsm + GradLayout<T, TC>::base(a.nslots, a.nl, a.n_internal));   // [K][K]
+    T *Ubuf = reinterpret_cast<T *>(gsm + Layout::base(a.nslots, a.nl, a.n_internal));   // [K][K]
     T *Pt = (a.nslots >= 2) ? slots : Ubuf + K2;                   // [K][TC]
     T *Qt = Pt + K * TC;                                           // [K][TC]
     T *Hbuf = Mat + K2;                                            // [K][K]
@@ -89,14 +96,25 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad(GradArgs a)
     const int a0 = 4 * ty, c0 = CPT * tx;
     const int nl = a.nl, n = 2 * nl - 1;
     unsigned char *sbase = reinterpret_cast<unsigned char *>(a.scratch) + (size_t)blockIdx.x * a.scratch_per_cta;
-    T *V = reinterpret_cast<T *>(sbase);                             // [n-1][K][TC]
-    T *B = V + (size_t)(n - 1) * K * TC;                             // [nl-1][K][TC] (internal nodes)
+    T *V = reinterpret_cast<T *>(sbase);                             // [nv][K][TC] child partials (vslot)
+    T *B = V + Layout::nv(nl) * K * TC;                              // [nl-1][K][TC] (internal nodes)
     int *eS = reinterpret_cast<int *>(B + (size_t)(nl - 1) * K * TC);  // [n][TC]
     int *fS = eS + (size_t)n * TC;                                   // [n][TC]
-    T *Ascr = reinterpret_cast<T *>(sbase + ((sizeof(T) * ((size_t)(n - 1) + (nl - 1)) * K * TC +
+    T *Ascr = reinterpret_cast<T *>(sbase + ((sizeof(T) * (Layout::nv(nl) + (nl - 1)) * K * TC +
                                               sizeof(int) * 2 * (size_t)n * TC + 255) & ~size_t(255)));   // [nl-1][K][TC]
+    // a child's slab among the stored partials (RECOMP: internal children only)
+    auto vslot = [&](int c) -> size_t { return RECOMP ? (size_t)(c - nl) : (size_t)c; };
     const int gstride = a.nbr + a.npar;
     auto e_of = [&](int node, int col) -> int { return node < nl ? 0 : eS[(size_t)node * TC + col]; };
+    // partial of child c at its parent, state st, tile column col: stored, or (RECOMP, a
+    // leaf) recomputed exactly as the inside pass formed it (child_partial: E^T[s][st] +
+    // delta, in one rounding; 1 for a marginalised leaf)
+    auto vpart = [&](const T *Pbase, int c, int st, int col) -> T {
+        if (!RECOMP || c >= nl) return V[(vslot(c) * K + st) * TC + col];
+        const int sl = lvT[c * TC + col];
+        if (sl >= K) return (T)1;
+        return fma(Pbase[(size_t)c * K2 + (size_t)sl * K + st], (T)1, sl == st ? (T)1 : (T)0);
+    };
 
     for (int f = tid; f < a.n_internal; f += GR_THREADS) sched[f] = a.sched[f];
 
@@ -146,8 +164,8 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad(GradArgs a)
             for (int i = 0; i < 4; i++)
 #pragma unroll
                 for (int cc = 0; cc < CPT; cc++) {
-                    V[((size_t)sn.lc * K + a0 + i) * TC + c0 + cc] = vl[i][cc];
-                    V[((size_t)sn.rc * K + a0 + i) * TC + c0 + cc] = vr[i][cc];
+                    if (!RECOMP || sn.lc >= nl) V[(vslot(sn.lc) * K + a0 + i) * TC + c0 + cc] = vl[i][cc];
+                    if (!RECOMP || sn.rc >= nl) V[(vslot(sn.rc) * K + a0 + i) * TC + c0 + cc] = vr[i][cc];
                 }
             __syncthreads();   // Mat and slots reads done; colmax zeroed
 #pragma unroll
@@ -247,18 +265,16 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad(GradArgs a)
                     }
                 }
                 for (int f = tid; f < TC; f += GR_THREADS) colmax[f] = 0;
-                const T *Vs = V + (size_t)s * K * TC;
-                for (int f = tid; f < K * TC; f += GR_THREADS) X[f] = Bp[f] * Vs[f];
+                for (int f = tid; f < K * TC; f += GR_THREADS) X[f] = Bp[f] * vpart(Pbase, s, f / TC, f % TC);
                 __syncthreads();
                 // gradient: (Q^T inter) . v_c per column, summed over this thread's 4 states
                 T wq[4][CPT];
                 contract<T, TC, KAHAN>(Mat + 2 * K2, X, a0, c0, wq);
-                const T *Vc = V + (size_t)c * K * TC;
 #pragma unroll
                 for (int cc = 0; cc < CPT; cc++) {
                     T acc = (T)0;
 #pragma unroll
-                    for (int i = 0; i < 4; i++) acc += wq[i][cc] * Vc[(size_t)(a0 + i) * TC + c0 + cc];
+                    for (int i = 0; i < 4; i++) acc += wq[i][cc] * vpart(Pbase, c, a0 + i, c0 + cc);
                     red[ty * TC + c0 + cc] = acc;
                 }
                 T bt[4][CPT];
@@ -370,26 +386,33 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad(GradArgs a)
     }
 }
 
-size_t grad_scratch_per_cta(int prec, int nl, int npar)
+size_t grad_scratch_per_cta(int prec, int nl, int npar, bool recompute_leaves)
 {
-    if (prec == PCSF_PREC_FP64) return GradLayout<double, 32>::scratch(nl, npar);
-    return GradLayout<float, 64>::scratch(nl, npar);
+    if (prec == PCSF_PREC_FP64)
+        return recompute_leaves ? GradLayout<double, 32, true>::scratch(nl, npar) : GradLayout<double, 32, false>::scratch(nl, npar);
+    return recompute_leaves ? GradLayout<float, 64, true>::scratch(nl, npar) : GradLayout<float, 64, false>::scratch(nl, npar);
 }
 
 size_t grad_smem_bytes(int prec, int nslots, int nl, int nint, int npar)
 {
-    if (prec == PCSF_PREC_FP64) return GradLayout<double, 32>::smem(nslots, nl, nint, npar);
-    return GradLayout<float, 64>::smem(nslots, nl, nint, npar);
+    if (prec == PCSF_PREC_FP64) return GradLayout<double, 32, false>::smem(nslots, nl, nint, npar);
+    return GradLayout<float, 64, false>::smem(nslots, nl, nint, npar);
+}
+
+template <typename T, int TC, int KAHAN, bool RECOMP>
+static cudaError_t launch_grad_r(const GradArgs &a, cudaStream_t s, int grid)
+{
+    size_t smem = GradLayout<T, TC, RECOMP>::smem(a.nslots, a.nl, a.n_internal, a.npar);
+    cudaError_t e = cudaFuncSetAttribute(k_grad<T, TC, KAHAN, RECOMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_grad<T, TC, KAHAN, RECOMP><<<grid, GR_THREADS, smem, s>>>(a);
+    return cudaGetLastError();
 }
 
 template <typename T, int TC, int KAHAN>
 static cudaError_t launch_grad_t(const GradArgs &a, cudaStream_t s, int grid)
 {
-    size_t smem = GradLayout<T, TC>::smem(a.nslots, a.nl, a.n_internal, a.npar);
-    cudaError_t e = cudaFuncSetAttribute(k_grad<T, TC, KAHAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k_grad<T, TC, KAHAN><<<grid, GR_THREADS, smem, s>>>(a);
-    return cudaGetLastError();
+    return a.recompute_leaves ? launch_grad_r<T, TC, KAHAN, true>(a, s, grid) : launch_grad_r<T, TC, KAHAN, false>(a, s, grid);
 }
 
 cudaError_t launch_grad(int prec, int comp, const GradArgs &a, cudaStream_t s, int grid)

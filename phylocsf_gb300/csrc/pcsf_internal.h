@@ -148,9 +148,10 @@ struct GradArgs {
     int npar;                // 0 or 2
     const void *Hmat;        // [pset][nbr][npar][K][K] (F(t_c) o Bdot_x)^T, arithmetic type
     const void *Umat;        // [model][K][K] U row-major, arithmetic type
+    int recompute_leaves;    // leaf children's partials recomputed in the outside pass, not stored
 };
 cudaError_t launch_grad(int prec, int comp, const GradArgs &a, cudaStream_t s, int grid);
-size_t grad_scratch_per_cta(int prec, int nl, int npar);
+size_t grad_scratch_per_cta(int prec, int nl, int npar, bool recompute_leaves);
 size_t grad_smem_bytes(int prec, int nslots, int nl, int nint, int npar);
 // H_x = (F(t) o Bdot_x)^T for every (P set, branch, parameter): F_ij = (e^{lam_i t} - e^{lam_j t}) /
 // (lam_i - lam_j), t e^{lam_i t} on the diagonal (Frechet derivative of exp in the eigenbasis)

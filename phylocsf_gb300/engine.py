@@ -124,6 +124,8 @@ SIGNATURES = {
     "pcsf_engine_exact_available": ([_VP], ctypes.c_int),
     "pcsf_engine_autotune": ([_VP, _VP, _I32], ctypes.c_int),
     "pcsf_engine_set_tc_shape": ([_VP, ctypes.c_int32], ctypes.c_int),
+    "pcsf_engine_set_grad_recompute": ([_VP, ctypes.c_int32], ctypes.c_int),
+    "pcsf_engine_grad_scratch_bytes": ([_VP, ctypes.c_int32], ctypes.c_int64),
     "pcsf_engine_tc_shape_times": ([_VP, _D, ctypes.c_int32], ctypes.c_int),
     "pcsf_engine_pt_search": ([_VP, ctypes.c_int32, ctypes.c_int32, _D, _D, _I32], ctypes.c_int),
     "pcsf_branch_counts": ([_VP, _VP, ctypes.c_int32, _D, _D, _D, _I32], ctypes.c_int),
@@ -482,6 +484,17 @@ class Engine:
         return P, st
 
     TC_SHAPES = {0: "alpha kept in registers", 1: "alpha read back"}
+
+    def set_grad_recompute(self, on: bool) -> None:
+        """Adjoint: recompute leaf children's partials instead of storing them (identical values)."""
+        _check(self.lib.pcsf_engine_set_grad_recompute(self.handle, 1 if on else 0), self.handle)
+
+    def grad_scratch_bytes(self, n_rate_params: int = 0) -> int:
+        """Adjoint scratch per CTA under the current setting."""
+        v = self.lib.pcsf_engine_grad_scratch_bytes(self.handle, n_rate_params)
+        if v < 0:
+            raise ValueError("n_rate_params must be 0 or 2")
+        return v
 
     def set_tc_shape(self, shape: int) -> None:
         """Shape of the TF32 tensor-core search kernel (TC_SHAPES; identical values)."""
