@@ -187,13 +187,11 @@ __device__ inline void contract(const T *M, const T *X, int a0, int c0, T out[4]
             comp[i][cc] = (T)0;
         }
     if (COMP == 2) {
-#pragma unroll 1
-        for (int jb = 0; jb < K; jb += 8) {
-            T g[4][CPT];
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int cc = 0; cc < CPT; cc++) g[i][cc] = (T)0;
+        // a block's sum starts from its first product (0 + p rounds as p does), and the
+        // first block is the running sum itself (its fold into zeros is exact, with a
+        // zero correction): the same values as zero-initialised sums and folds, with
+        // fewer instructions in this issue-bound loop
+        auto block = [&](int jb, T g[4][CPT]) {
 #pragma unroll
             for (int j = jb; j < jb + 8; j++) {
                 T e[4], x[CPT];
@@ -202,8 +200,14 @@ __device__ inline void contract(const T *M, const T *X, int a0, int c0, T out[4]
 #pragma unroll
                 for (int i = 0; i < 4; i++)
 #pragma unroll
-                    for (int cc = 0; cc < CPT; cc++) g[i][cc] += e[i] * x[cc];
+                    for (int cc = 0; cc < CPT; cc++) g[i][cc] = (j == jb) ? e[i] * x[cc] : fma(e[i], x[cc], g[i][cc]);
             }
+        };
+        block(0, out);
+#pragma unroll 1
+        for (int jb = 8; jb < K; jb += 8) {
+            T g[4][CPT];
+            block(jb, g);
 #pragma unroll
             for (int i = 0; i < 4; i++)
 #pragma unroll
