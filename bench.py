@@ -626,11 +626,24 @@ def run_omega(args, world, rank, local):
         t0 = time.perf_counter()
         g64 = e64.omega_grad(b64, wl.kappa, wl.omega[sub], 1.0, wl.sigma)
         t64 = time.perf_counter() - t0
-        rel = {}
+        # the gradient is taken at the simulated parameters, near the optimum, where the true
+        # derivatives are small: besides the relative error (floor 1e-2) report the absolute
+        # error and the absolute error over sqrt(columns), the scale of the derivative's
+        # column-to-column fluctuation
+        rel, med, absmax, per_sqrt = {}, {}, {}, {}
+        ncol = np.diff(so).astype(np.float64)
         for k in ("d_kappa", "d_omega", "d_rho", "d_branch"):
             a, c = g64[k], g[k][sub]
-            rel[k] = float(np.max(np.abs(c - a) / (np.abs(a) + 1e-2)))
+            err = np.abs(c - a)
+            r = err / (np.abs(a) + 1e-2)
+            rel[k] = float(np.max(r))
+            med[k] = float(np.median(r))
+            absmax[k] = float(np.max(err))
+            scale = np.sqrt(ncol).reshape((-1,) + (1,) * (err.ndim - 1))
+            per_sqrt[k] = float(np.max(err / scale))
         line["accuracy"] = {"vs_fp64_gpu": {"alignments": int(len(sub)), "max_rel_error": rel,
+                                            "median_rel_error": med, "max_abs_error": absmax,
+                                            "max_abs_error_per_sqrt_column": per_sqrt,
                                             "lpr_max_rel": float(np.max(np.abs(g["lpr"][sub] - g64["lpr"]) /
                                                                         np.abs(g64["lpr"])))},
                             "fp64_seconds_on_sample": t64}
