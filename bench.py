@@ -324,6 +324,39 @@ def make_spec(args, seed):
     return spec
 
 
+def measure_matmul_peaks(local):
+    """Dense GEMM throughput of this GPU for the arithmetic types the kernels use but the
+    driver's peak file does not cover: TF32 tensor cores (the search's products), FP32 on
+    the CUDA cores (the SIMT kernels) and FP64 (the FP64 engine); cuBLAS through torch,
+    best of 5 CUDA-event-timed multiplies after 2 warm-ups, 2 n^3 FLOPs each."""
+    import torch
+    dev = torch.device("cuda", local)
+    keep = (torch.backends.cuda.matmul.allow_tf32, torch.backends.cudnn.allow_tf32)
+    out = {}
+    try:
+        for name, dt, tf32, n in (("tf32", torch.float32, True, 8192), ("fp32", torch.float32, False, 8192),
+                                  ("fp64", torch.float64, False, 4096)):
+            torch.backends.cuda.matmul.allow_tf32 = tf32
+            a = torch.randn(n, n, dtype=dt, device=dev)
+            b = torch.randn(n, n, dtype=dt, device=dev)
+            c = torch.empty(n, n, dtype=dt, device=dev)
+            for _ in range(2):
+                torch.matmul(a, b, out=c)
+            best = 1e30
+            for _ in range(5):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                torch.matmul(a, b, out=c)
+                e1.record()
+                e1.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            out[name + "_tflops"] = 2.0 * n ** 3 / (best / 1000.0) / 1e12
+            del a, b, c
+    finally:
+        torch.backends.cuda.matmul.allow_tf32, torch.backends.cudnn.allow_tf32 = keep
+    return out
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -367,6 +400,7 @@ def run_ours(args, world, rank, local):
     tc_shape_ms = None
     if tile is not None and eng.stats()["tc_shape"] >= 0:
         tc_shape_ms = {P.Engine.TC_SHAPES[k]: round(float(v), 3) for k, v in enumerate(eng.tc_shape_times())}
+    gemm_peaks = measure_matmul_peaks(local) if rank == 0 else {}
 
     # inputs smaller than twice the L2 (129 MB) get an L2 flush before every timed step
     flush = None
@@ -440,6 +474,9 @@ def run_ours(args, world, rank, local):
     peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
     sm_mhz = (clk or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    # the TF32 search executes three products per contraction (hi x hi, hi x lo, lo x hi)
+    nprod = {"tf32x3": 3, "tf32x3b": 3, "tf32x3_direct": 3, "tf32": 1, "tf32_direct": 1}.get(args.precision)
+    tf32_measured = gemm_peaks.get("tf32_tflops")
     traffic = load_traffic(KERNEL_KEYS[kind])
     traffic_per_launch = (traffic * kcols / launches) if traffic else None
     shares = {KERNEL_KEYS[k]: st["kind_ms"][k] / args.steps for k in range(NKINDS)}
@@ -473,7 +510,11 @@ def run_ours(args, world, rank, local):
                          "peak_kind": peak_kind + " bf16 sustained",
                          "traffic": traffic_per_launch, "alg_flops_per_launch": kflops / launches,
                          "avg_launch_ms": kms / launches, "launches": int(launches),
-                         "fp32_fma_peak_tflops": fp32_peak, "frac_of_fp32_fma_peak": achieved_tflops / fp32_peak},
+                         "fp32_fma_peak_tflops": fp32_peak, "frac_of_fp32_fma_peak": achieved_tflops / fp32_peak,
+                         "gemm_peaks_measured": {k: round(v, 2) for k, v in gemm_peaks.items()},
+                         "executed_tf32_tflops": (nprod * achieved_tflops if kind == 1 and nprod else None),
+                         "frac_executed_of_tf32_measured": (nprod * achieved_tflops / tf32_measured
+                                                            if kind == 1 and nprod and tf32_measured else None)},
             "kernel_ms_per_step": dict(shares, other=st["other_ms"] / args.steps),
             "pruning_kernels": kinds,
             "clocks": clk}
