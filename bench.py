@@ -516,6 +516,14 @@ def run_ours(args, world, rank, local):
                          "frac_executed_of_tf32_measured": (nprod * achieved_tflops / tf32_measured
                                                             if kind == 1 and nprod and tf32_measured else None)},
             "kernel_ms_per_step": dict(shares, other=st["other_ms"] / args.steps),
+            # P(t) formation as its own line: 2 * 64^3 FLOPs per branch of every P set when done
+            # as GEMMs; one P set per (region, model, rho) evaluation at most (P sets are shared
+            # by requests with the same model and rho), so this is an upper bound
+            "pform": {"ms_per_step": st["pform_ms"] / args.steps, "launches_per_step": st["pform_launches"] / args.steps,
+                      "psets_per_step_at_most": st["evaluations"] / args.steps,
+                      "gemm_flops_per_pset": 2 * 64 ** 3 * nb,
+                      "tflops_at_most": (st["evaluations"] * 2 * 64 ** 3 * nb / (st["pform_ms"] / 1000.0) / 1e12
+                                         if st["pform_ms"] > 0 else None)},
             "pruning_kernels": kinds,
             "clocks": clk}
 
