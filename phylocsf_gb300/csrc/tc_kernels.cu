@@ -360,6 +360,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
             }
         };
         int escale = 0;     // this column's sum of rescale exponents
+        bool pend_bad = false;   // a timed-out wait seen since the last CTA-wide barrier
         int kc = 0;         // contractions so far (index into bseq / dreg)
 
         for (int ni = 0; ni < a.n_internal && ok; ni++) {
@@ -393,7 +394,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
                 stage_a(s, r >= 0, al);
                 if (tid == 0 && !wait_b()) bad = true;
                 tc_fence_before();
-                if (__syncthreads_or(bad)) { ok = false; break; }
+                if (__syncthreads_or(bad || pend_bad)) { ok = false; break; }
                 tc_fence_after();
                 if (tid == 0) issue_mma(s, r);
                 prefetch_next(ni);      // while the MMAs run
@@ -423,7 +424,12 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
             for (int k = 0; k < 32; k++) mx = fmaxf(mx, v[k]);
             float (*cm)[TCP_M] = cmax[ni & 1];          // double-buffered: no second barrier needed
             cm[half][site] = mx;
-            if (__syncthreads_or(bad)) { ok = false; break; }
+            // only warps w and w + 4 share these columns: a named barrier of those 64 threads
+            // (barriers 1-4; both warps walk the same schedule, so both always arrive).  A
+            // timed-out wait is carried to the next CTA-wide barrier (the next staging, or the
+            // root), which every thread reaches before any further MMA is issued.
+            asm volatile("bar.sync %0, 64;" :: "r"(1 + (warp & 3)) : "memory");
+            pend_bad |= bad;
             mx = fmaxf(cm[0][site], cm[1][site]);
             const int e = (mx > 0.0f) ? exp_of(mx) : 0;
             escale += e;
@@ -445,6 +451,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 2) k_prune_tc(PruneArgs a, uint32
         // prior * log prior in FP32)
         float *zpart = reinterpret_cast<float *>(sm + SM_A);
         float *prf = zpart + 4 * TCP_M, *wlf = prf + K;
+        if (__syncthreads_or(pend_bad)) { ok = false; break; }   // every warp is past its last node
         if (tid < K) {
             prf[tid] = (float)a.m.prior[md * K + tid];
             wlf[tid] = (float)a.m.wlog[md * K + tid];
