@@ -193,6 +193,14 @@ int pcsf_engine_exact_available(const pcsf_engine *e);
  * No reference counterpart (the reference has no device). */
 int pcsf_engine_autotune(pcsf_engine *e, pcsf_batch *b, int32_t *tile);
 
+/* Derivative of the search values for the derivative rule of reduced-precision mle
+ * searches (a trial point within 1e-4 |x| of the best point x is valued as
+ * f(x) + f'(x)(u - x)): mode 1 = central difference of two search evaluations at
+ * x (1 +- 2e-3) (the default of tensor-core engines: about half the cost of the
+ * tangent pass), 0 = the analytic derivative (the tensor-core tangent pass where the
+ * tree fits it, else the adjoint; the default of the other engines). */
+int pcsf_engine_set_derivative_mode(pcsf_engine *e, int32_t mode);
+
 /* Adjoint memory (pcsf_grad, pcsf_omega_grad and the derivative rule of engines without
  * the tangent pass): with on != 0 the outside pass recomputes the partials of leaf
  * children (one gathered row of P each) instead of storing them, a third less scratch

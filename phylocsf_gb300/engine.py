@@ -125,6 +125,7 @@ SIGNATURES = {
     "pcsf_engine_autotune": ([_VP, _VP, _I32], ctypes.c_int),
     "pcsf_engine_set_tc_shape": ([_VP, ctypes.c_int32], ctypes.c_int),
     "pcsf_engine_set_grad_recompute": ([_VP, ctypes.c_int32], ctypes.c_int),
+    "pcsf_engine_set_derivative_mode": ([_VP, ctypes.c_int32], ctypes.c_int),
     "pcsf_engine_grad_scratch_bytes": ([_VP, ctypes.c_int32], ctypes.c_int64),
     "pcsf_engine_tc_shape_times": ([_VP, _D, ctypes.c_int32], ctypes.c_int),
     "pcsf_engine_pt_search": ([_VP, ctypes.c_int32, ctypes.c_int32, _D, _D, _I32], ctypes.c_int),
@@ -484,6 +485,11 @@ class Engine:
         return P, st
 
     TC_SHAPES = {0: "alpha kept in registers", 1: "alpha read back"}
+
+    def set_derivative_mode(self, mode: int) -> None:
+        """Search derivative of the mle derivative rule: 1 central difference of search values
+        (tensor-core default), 0 analytic (tangent pass or adjoint)."""
+        _check(self.lib.pcsf_engine_set_derivative_mode(self.handle, mode), self.handle)
 
     def set_grad_recompute(self, on: bool) -> None:
         """Adjoint: recompute leaf children's partials instead of storing them (identical values)."""
