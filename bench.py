@@ -555,7 +555,8 @@ def run_ours(args, world, rank, local):
                            "clock": "host wall clock around each call (synchronous API)"}
     if rank == 0 and not args.no_fp64:
         # the plain FP64 GPU path (oracle-matched iterates) on a length-stratified sample: the
-        # the benchmark spec's denominator (time) and the accuracy reference (scores)
+        # path the split-precision engine is compared against (time) and the accuracy
+        # reference (scores)
         sub = stratified(wl.col_offsets, args.fp64_regions)
         parts = [wl.leaves[wl.col_offsets[i]:wl.col_offsets[i + 1]] for i in sub]
         so = np.zeros(len(sub) + 1, np.int64)
